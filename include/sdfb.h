@@ -1,0 +1,176 @@
+/*
+ * sdfb.h -- C ABI of the GB300 mesh -> signed-distance-field bake.
+ *
+ * This is the drop-in boundary for the reference's bake path. Every entry point takes plain
+ * pointers and sizes, returns an sdfb_status, and never throws across the ABI. The reference
+ * interface each one replaces is cited beside it (paths inside the reference project).
+ *
+ * Conventions
+ *   - Grids are dense, x-fastest: cell (x, y, z) is at (z * ny + y) * nx + x
+ *     (src/convert/sdf_grid.h:35). The sample point of a cell is its FP32 centre
+ *     origin + (float(i) + 0.5f) * voxel_size per axis (src/render/kernels/sdf_bake.cu:34-37,
+ *     src/convert/sdf_baker.cpp:107).
+ *   - Distances are FP32, negative inside (sdf_bake.cu:69-72). Occupancy is uint8 0/1: a cell is
+ *     occupied when a triangle whose clamped cell range contains it passes the triangle/box
+ *     separating-axis test (sdf_baker.cpp:89-118, tri_box_overlap.h:72-114).
+ *   - Meshes are indexed: verts is V x 3 FP32, idx is T x 3 uint32. The soup entry point takes the
+ *     reference's MeshAsset layout (3 positions per triangle, src/io/mesh_asset.h:33-46).
+ *   - A context owns one device, its streams, device memory and the resident mesh cache. Use one
+ *     context from one host thread at a time; separate contexts are independent.
+ *   - On an error the entry point returns a non-zero status and sdfb_last_error(ctx) describes it
+ *     (the reference throws std::runtime_error from OPTIX_CHECK / CUDA_CHECK,
+ *     src/render/optix_check.h:13-52).
+ */
+#ifndef SDFB_H
+#define SDFB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SDFB_ABI_VERSION 1
+
+typedef enum sdfb_status {
+  SDFB_OK = 0,
+  SDFB_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size, bad grid */
+  SDFB_ERR_OUT_OF_MEMORY = 2,    /* device or pinned host allocation failed, or over a budget */
+  SDFB_ERR_CUDA = 3,             /* a CUDA runtime call failed (message in sdfb_last_error) */
+  SDFB_ERR_BAD_MESH = 4,         /* triangle index >= V, or a non-finite vertex */
+  SDFB_ERR_OVERFLOW = 5,         /* a bounded device structure overflowed (traversal stack) */
+  SDFB_ERR_BUSY = 6,             /* serving: no slot or memory free right now */
+  SDFB_ERR_TIMEOUT = 7,          /* serving: a wait ran out */
+  SDFB_ERR_NOT_FOUND = 8,        /* serving: unknown mesh or request id */
+  SDFB_ERR_NO_DEVICE = 9,        /* no CUDA device, or the device is not sm_103 */
+  SDFB_ERR_INTERNAL = 10
+} sdfb_status;
+
+/* Sign modes. AUTO welds the mesh (src/io/mesh_weld.cpp:26-48) and runs the watertight test
+ * (src/io/mesh_validate.cpp:21-59): watertight meshes use PARITY, others GWN. */
+typedef enum sdfb_sign_mode {
+  SDFB_SIGN_AUTO = 0,
+  SDFB_SIGN_PARITY = 1, /* exact +z ray parity, robust predicates */
+  SDFB_SIGN_GWN = 2,    /* generalized winding number, |w| > 0.5 is inside */
+  SDFB_SIGN_NONE = 3    /* unsigned distance */
+} sdfb_sign_mode;
+
+typedef struct sdfb_ctx sdfb_ctx;
+
+/* Dense grid description (the reference's SdfGrid origin / voxelSize / nx, ny, nz,
+ * src/convert/sdf_grid.h:21-26). */
+typedef struct sdfb_grid_desc {
+  float origin[3];
+  float voxel_size;
+  int32_t nx, ny, nz;
+} sdfb_grid_desc;
+
+/* Bake options. Zero-initialise and set struct_size = sizeof(sdfb_opts); zero fields take the
+ * defaults named beside them. */
+typedef struct sdfb_opts {
+  uint32_t struct_size;
+  int32_t sign_mode;      /* sdfb_sign_mode, default AUTO */
+  float band_voxels;      /* GWN: width in voxels of the FP64 band around the surface, default 1 */
+  int32_t leaf_size;      /* BVH leaf size 1..16, default: autotuned table */
+  int32_t tile;           /* distance tile shape id (see sdfb_tile_count), default: autotuned */
+  int32_t no_occupancy;   /* 1: skip occupancy (occ_out may be NULL) */
+  int32_t no_distance;    /* 1: occupancy only (dist_out may be NULL) */
+  int32_t count_work;     /* 1: count traversal work into stats (a slower, instrumented kernel) */
+  int32_t reserved[8];
+} sdfb_opts;
+
+/* Per-call statistics, filled when the pointer is non-null. Times are CUDA-event times on the
+ * bake stream (ms); counts are exact. */
+typedef struct sdfb_stats {
+  uint32_t struct_size;
+  int32_t sign_mode_used;
+  int32_t watertight;      /* 1, 0, or -1 when not evaluated */
+  int32_t leaf_size_used;
+  int32_t tile_used;
+  int32_t pad0;
+  double ms_total;         /* first to last event on the device */
+  double ms_prepare;       /* validation, triangle layout, bounds */
+  double ms_build;         /* Morton codes, sort, hierarchy, refit */
+  double ms_occupancy;
+  double ms_sign;          /* parity crossings or winding-number band */
+  double ms_distance;      /* nearest-triangle traversal (+ fused sign) */
+  uint64_t voxels;
+  uint64_t triangles;
+  uint64_t sat_tests;      /* triangle/box tests run by the occupancy kernel */
+  uint64_t crossings;      /* parity crossings found */
+  uint64_t box_tests;      /* point-box tests (lanes) when opts.count_work = 1 */
+  uint64_t tri_tests;      /* point-triangle tests (lanes) when opts.count_work = 1 */
+  double flops_distance;   /* FP32 flops of those tests (FMA = 2) */
+  uint64_t reserved[5];
+} sdfb_stats;
+
+/* ---- context ---------------------------------------------------------------------------- */
+
+/* Creates a context on CUDA device `device` (sm_103 required). */
+sdfb_status sdfb_ctx_create(int32_t device, sdfb_ctx **out);
+void sdfb_ctx_destroy(sdfb_ctx *ctx);
+/* Last error text of the context (empty when none); valid until the next call on ctx. */
+const char *sdfb_last_error(const sdfb_ctx *ctx);
+/* Library ABI version (SDFB_ABI_VERSION). */
+int32_t sdfb_abi_version(void);
+/* Releases cached device memory that no live object uses. */
+sdfb_status sdfb_ctx_trim(sdfb_ctx *ctx);
+/* Bytes of device memory the context holds (cached buffers and resident meshes). */
+uint64_t sdfb_ctx_device_bytes(const sdfb_ctx *ctx);
+
+/* ---- grids (bakeSdf sizing, src/convert/sdf_baker.cpp:138-148) -------------------------- */
+
+/* voxel = max(extent, 1e-6) / max(res, 1); origin = bmin - 2 voxel;
+ * n_axis = ceil((extent_axis + 4 voxel) / voxel) + 1, all in FP32 as the reference does. */
+sdfb_status sdfb_grid_from_bounds_res(const float bmin[3], const float bmax[3], int32_t resolution,
+                                      sdfb_grid_desc *out);
+
+/* ---- plain bake (replaces italy::bakeSdf, src/convert/sdf_baker.h:8) --------------------- */
+
+/* Synchronous bake from host buffers. dist_out holds nx*ny*nz floats, occ_out nx*ny*nz bytes;
+ * either may be NULL to skip that output. opts and stats may be NULL. */
+sdfb_status sdfb_bake(sdfb_ctx *ctx, const float *verts, uint32_t num_verts, const uint32_t *idx,
+                      uint32_t num_tris, const sdfb_grid_desc *grid, const sdfb_opts *opts, float *dist_out,
+                      uint8_t *occ_out, sdfb_stats *stats);
+
+/* Same bake with every buffer already in device memory of the context's device. Work is
+ * enqueued on `stream` (a cudaStream_t, NULL = the context's stream); the call returns after the
+ * work completes and its error flags are read. */
+sdfb_status sdfb_bake_device(sdfb_ctx *ctx, const float *d_verts, uint32_t num_verts, const uint32_t *d_idx,
+                             uint32_t num_tris, const sdfb_grid_desc *grid, const sdfb_opts *opts,
+                             float *d_dist_out, uint8_t *d_occ_out, void *stream, sdfb_stats *stats);
+
+/* MeshAsset-layout bake (src/convert/sdf_baker.cpp:137-310): `positions` holds 9 floats per
+ * triangle; the grid is sized from bounds and resolution exactly as bakeSdf does and written to
+ * grid_out. Call once with dist_out = occ_out = NULL to learn the grid, then again with buffers
+ * of grid_out->nx * ny * nz elements. */
+sdfb_status sdfb_bake_soup(sdfb_ctx *ctx, const float *positions, uint32_t num_tris, const float bounds_min[3],
+                           const float bounds_max[3], int32_t resolution, const sdfb_opts *opts,
+                           sdfb_grid_desc *grid_out, float *dist_out, uint8_t *occ_out, sdfb_stats *stats);
+
+/* ---- sparse voxelization (replaces italy::voxelizeMesh, src/convert/voxelize.h:8) -------- */
+
+/* `positions` holds 9 floats per triangle. origin = bounds_min, voxel = longest / res, cells in
+ * the reference's insertion order (voxelize.cpp:52-107). Writes min(count, cap) cells (3 int32
+ * each) and returns the full count in *count. */
+sdfb_status sdfb_voxelize_sparse(sdfb_ctx *ctx, const float *positions, uint32_t num_tris, const float bounds_min[3],
+                                 const float bounds_max[3], int32_t resolution, int32_t *cells_out, uint64_t cap,
+                                 uint64_t *count, float origin_out[3], float *voxel_out);
+
+/* ---- mesh utilities (src/io/mesh_weld.cpp:26-48, src/io/mesh_validate.cpp:21-59) -------- */
+
+/* Welds positions on the max(|extent| * 1e-5, 1e-6) lattice; welded_out gets one index per
+ * position (first-occurrence numbering), *num_unique the number of distinct vertices. */
+sdfb_status sdfb_weld(sdfb_ctx *ctx, const float *positions, uint32_t num_positions, const float bounds_min[3],
+                      const float bounds_max[3], uint32_t *welded_out, uint32_t *num_unique);
+/* Watertight test over a welded index buffer (3 per triangle): *watertight = 1 when no edge is
+ * used once (boundary) or more than twice (non-manifold); degenerate triangles are skipped. */
+sdfb_status sdfb_is_watertight(sdfb_ctx *ctx, const uint32_t *welded_idx, uint32_t num_tris, int32_t *watertight,
+                               uint64_t *boundary_edges, uint64_t *nonmanifold_edges);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SDFB_H */

@@ -1,0 +1,280 @@
+// Device-side building blocks shared by the bake kernels (sm_103a).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sdfb {
+
+// ---------------------------------------------------------------------------------------------
+// Error flags raised by kernels (OR-ed into one device word, read by the host after a bake).
+enum DevErr : uint32_t {
+  kErrBadIndex = 1u,          // triangle index >= V
+  kErrNonFinite = 2u,         // vertex with NaN / Inf coordinate
+  kErrStackOverflow = 4u,     // traversal stack exhausted
+  kErrCrossingOverflow = 8u,  // parity crossing list exceeded its capacity
+  kErrEmpty = 16u,
+};
+
+constexpr int kWarp = 32;
+constexpr uint32_t kFull = 0xffffffffu;
+
+// ---------------------------------------------------------------------------------------------
+// Cell centre, exactly as the reference rounds it: origin + (float(i) + 0.5f) * voxel, with no
+// fused multiply-add (src/convert/sdf_baker.cpp:107, src/render/kernels/sdf_bake.cu:34-37).
+__device__ __forceinline__ float cell_center(float origin, int i, float voxel) {
+  return __fadd_rn(origin, __fmul_rn(__fadd_rn(__int2float_rn(i), 0.5f), voxel));
+}
+
+// float -> int after floor, saturating, NaN -> 0 (cvt.rzi.s32.f32).
+__device__ __forceinline__ int f2i_sat(float f) { return __float2int_rz(f); }
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// std::min / std::max as the reference evaluates them.
+__device__ __forceinline__ float min_ref(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float max_ref(float a, float b) { return (a < b) ? b : a; }
+
+// ---------------------------------------------------------------------------------------------
+// Triangle / box separating-axis test with the reference's exact FP32 rounding
+// (src/convert/tri_box_overlap.h:12-114): every product and sum is one IEEE operation, in the
+// reference's order, through the _rn intrinsics so that nothing contracts into an FMA. The
+// occupancy it defines must match the reference bit for bit.
+struct f3 {
+  float x, y, z;
+};
+
+__device__ __forceinline__ f3 sub3(f3 a, f3 b) { return {__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)}; }
+__device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+
+__device__ __forceinline__ bool axis_overlaps(float pa, float pb, float rad) {
+  const float mn = min_ref(pa, pb), mx = max_ref(pa, pb);
+  return !(mn > rad || mx < -rad);
+}
+// Edge (a, b) projections onto e x X, e x Y, e x Z in the reference's operand pairing.
+__device__ __forceinline__ float proj_x(float a, float b, f3 v) { return __fsub_rn(mul(a, v.y), mul(b, v.z)); }
+__device__ __forceinline__ float proj_y(float a, float b, f3 v) { return __fadd_rn(mul(-a, v.x), mul(b, v.z)); }
+__device__ __forceinline__ float proj_z(float a, float b, f3 v) { return __fsub_rn(mul(a, v.x), mul(b, v.y)); }
+__device__ __forceinline__ float rad2(float fa, float ha, float fb, float hb) { return __fadd_rn(mul(fa, ha), mul(fb, hb)); }
+__device__ __forceinline__ float dot_ref(f3 a, f3 b) {
+  return __fadd_rn(__fadd_rn(mul(a.x, b.x), mul(a.y, b.y)), mul(a.z, b.z));
+}
+
+__device__ __forceinline__ bool plane_box_overlap(f3 n, f3 v, float h) {
+  f3 vmin, vmax;
+  vmin.x = n.x > 0.0f ? __fsub_rn(-h, v.x) : __fsub_rn(h, v.x);
+  vmax.x = n.x > 0.0f ? __fsub_rn(h, v.x) : __fsub_rn(-h, v.x);
+  vmin.y = n.y > 0.0f ? __fsub_rn(-h, v.y) : __fsub_rn(h, v.y);
+  vmax.y = n.y > 0.0f ? __fsub_rn(h, v.y) : __fsub_rn(-h, v.y);
+  vmin.z = n.z > 0.0f ? __fsub_rn(-h, v.z) : __fsub_rn(h, v.z);
+  vmax.z = n.z > 0.0f ? __fsub_rn(h, v.z) : __fsub_rn(-h, v.z);
+  if (dot_ref(n, vmin) > 0.0f) return false;
+  return dot_ref(n, vmax) >= 0.0f;
+}
+
+// Box centre c, cubic half extent h (the reference always passes vec3(voxel * 0.5f)).
+__device__ __forceinline__ bool sat_overlap(f3 c, float h, f3 t0, f3 t1, f3 t2) {
+  const f3 v0 = sub3(t0, c), v1 = sub3(t1, c), v2 = sub3(t2, c);
+  const f3 e0 = sub3(v1, v0), e1 = sub3(v2, v1), e2 = sub3(v0, v2);
+  float fx = fabsf(e0.x), fy = fabsf(e0.y), fz = fabsf(e0.z);
+  if (!axis_overlaps(proj_x(e0.z, e0.y, v0), proj_x(e0.z, e0.y, v2), rad2(fz, h, fy, h))) return false;
+  if (!axis_overlaps(proj_y(e0.z, e0.x, v0), proj_y(e0.z, e0.x, v2), rad2(fz, h, fx, h))) return false;
+  if (!axis_overlaps(proj_z(e0.y, e0.x, v1), proj_z(e0.y, e0.x, v2), rad2(fy, h, fx, h))) return false;
+  fx = fabsf(e1.x); fy = fabsf(e1.y); fz = fabsf(e1.z);
+  if (!axis_overlaps(proj_x(e1.z, e1.y, v0), proj_x(e1.z, e1.y, v2), rad2(fz, h, fy, h))) return false;
+  if (!axis_overlaps(proj_y(e1.z, e1.x, v0), proj_y(e1.z, e1.x, v2), rad2(fz, h, fx, h))) return false;
+  if (!axis_overlaps(proj_z(e1.y, e1.x, v0), proj_z(e1.y, e1.x, v1), rad2(fy, h, fx, h))) return false;
+  fx = fabsf(e2.x); fy = fabsf(e2.y); fz = fabsf(e2.z);
+  if (!axis_overlaps(proj_x(e2.z, e2.y, v0), proj_x(e2.z, e2.y, v1), rad2(fz, h, fy, h))) return false;
+  if (!axis_overlaps(proj_y(e2.z, e2.x, v0), proj_y(e2.z, e2.x, v1), rad2(fz, h, fx, h))) return false;
+  if (!axis_overlaps(proj_z(e2.y, e2.x, v1), proj_z(e2.y, e2.x, v2), rad2(fy, h, fx, h))) return false;
+  if (min_ref(min_ref(v0.x, v1.x), v2.x) > h || max_ref(max_ref(v0.x, v1.x), v2.x) < -h) return false;
+  if (min_ref(min_ref(v0.y, v1.y), v2.y) > h || max_ref(max_ref(v0.y, v1.y), v2.y) < -h) return false;
+  if (min_ref(min_ref(v0.z, v1.z), v2.z) > h || max_ref(max_ref(v0.z, v1.z), v2.z) < -h) return false;
+  const f3 n = {__fsub_rn(mul(e0.y, e1.z), mul(e1.y, e0.z)), __fsub_rn(mul(e0.z, e1.x), mul(e1.z, e0.x)),
+                __fsub_rn(mul(e0.x, e1.y), mul(e1.x, e0.y))};
+  return plane_box_overlap(n, v0, h);
+}
+
+// Candidate cell range of a triangle along one axis: floor((min - origin) / voxel) clamped to
+// [0, nmax] (sdf_baker.cpp:97-101), IEEE division, saturating conversion.
+__device__ __forceinline__ int cell_index_clamped(float c, float origin, float voxel, int nmax) {
+  return clampi(f2i_sat(floorf(__fdiv_rn(__fsub_rn(c, origin), voxel))), 0, nmax);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Exact 2-D orientation with simulation of simplicity (parity sign).
+//
+// orient(a, b, p) = (b - a) x (p - a) for FP32 inputs. A FP32 evaluation is accepted when its
+// magnitude exceeds a forward error bound (Shewchuk 1997, the orient2d "A" bound with a safety
+// margin); otherwise the value is expanded into six products of inputs, each exact in FP64, and
+// the sign of their sum is found exactly with Two-Sum / Grow-Expansion. A zero value is broken as
+// if p were p + (eps, eps^2): the sign becomes that of (a_v - b_v), else (b_u - a_u).
+
+__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
+  const double x = __dadd_rn(a, b);
+  const double bv = __dsub_rn(x, a);
+  const double av = __dsub_rn(x, bv);
+  s = x;
+  e = __dadd_rn(__dsub_rn(a, av), __dsub_rn(b, bv));
+}
+
+static __device__ __noinline__ int exact_orient_sign(float au, float av, float bu, float bv, float pu, float pv) {
+  double t[6];
+  t[0] = __dmul_rn((double)bu, (double)pv);
+  t[1] = -__dmul_rn((double)bu, (double)av);
+  t[2] = -__dmul_rn((double)au, (double)pv);
+  t[3] = -__dmul_rn((double)bv, (double)pu);
+  t[4] = __dmul_rn((double)bv, (double)au);
+  t[5] = __dmul_rn((double)av, (double)pu);
+  double e[6];
+  int m = 1;
+  e[0] = t[0];
+#pragma unroll
+  for (int k = 1; k < 6; ++k) {
+    double q = t[k];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      if (i < m) {
+        double s, err;
+        two_sum(q, e[i], s, err);
+        e[i] = err;
+        q = s;
+      }
+    }
+    e[m++] = q;
+  }
+  int sign = 0;
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+    if (e[i] != 0.0) sign = e[i] > 0.0 ? 1 : -1;  // last non-zero = most significant
+  return sign;
+}
+
+// Returns the orientation sign (+1 / -1) and the FP32 value (for barycentric weights).
+__device__ __forceinline__ int orient2_sos(float au, float av, float bu, float bv, float pu, float pv, float &val) {
+  const float l = __fmul_rn(__fsub_rn(bu, au), __fsub_rn(pv, av));
+  const float r = __fmul_rn(__fsub_rn(bv, av), __fsub_rn(pu, au));
+  const float det = __fsub_rn(l, r);
+  val = det;
+  const float bound = 4.0f * 5.9604645e-8f * (fabsf(l) + fabsf(r));  // 4 * 2^-24 * (|l| + |r|)
+  if (fabsf(det) > bound && fabsf(det) > 1e-30f) return det > 0.0f ? 1 : -1;
+  const int s = exact_orient_sign(au, av, bu, bv, pu, pv);
+  if (s) return s;
+  if (av != bv) return av > bv ? 1 : -1;
+  if (bu != au) return bu > au ? 1 : -1;
+  return 0;
+}
+
+// Does the +z line through (px, py) cross triangle (a, b, c)? On a crossing *z receives the
+// crossing height (FP32 barycentric blend, within the triangle's z range).
+__device__ __forceinline__ bool column_crossing(f3 a, f3 b, f3 c, float px, float py, float &z) {
+  float wab, wbc, wca;
+  const int s0 = orient2_sos(a.x, a.y, b.x, b.y, px, py, wab);
+  if (s0 == 0) return false;
+  const int s1 = orient2_sos(b.x, b.y, c.x, c.y, px, py, wbc);
+  if (s1 != s0) return false;
+  const int s2 = orient2_sos(c.x, c.y, a.x, a.y, px, py, wca);
+  if (s2 != s0) return false;
+  const float wa = fabsf(wbc), wb = fabsf(wca), wc = fabsf(wab);
+  const float den = wa + wb + wc;
+  if (den > 0.0f) {
+    z = (wa * a.z + wb * b.z + wc * c.z) / den;
+    z = fminf(fmaxf(z, fminf(fminf(a.z, b.z), c.z)), fmaxf(fmaxf(a.z, b.z), c.z));
+  } else {
+    z = (a.z + b.z + c.z) * (1.0f / 3.0f);
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Triangle record for distance queries: 64 bytes, four float4s, in BVH leaf order.
+//   r0 = (v0, 1/|e1|^2)    e1 = v1 - v0
+//   r1 = (e1, 1/|e2|^2)    e2 = v2 - v0
+//   r2 = (e2, 1/|e3|^2)    e3 = v2 - v1
+//   r3 = (n,  1/|n|^2)     n = e1 x e2; 1/|n|^2 = 0 marks a degenerate triangle
+// Squared distance: inside the face's prism it is (ap . n)^2 / |n|^2, otherwise the minimum over
+// the three edges of |ap - clamp(ap . e / |e|^2, 0, 1) e|^2. Branch-free, so every lane of a warp
+// executes the same instructions for the same triangle.
+struct TriRec {
+  float4 r0, r1, r2, r3;
+};
+
+__device__ __forceinline__ float inv_or_zero(float x) { return x > 0.0f ? 1.0f / x : 0.0f; }
+
+__device__ __forceinline__ float seg_dist2(float px, float py, float pz, float ex, float ey, float ez, float inv_len2) {
+  float t = (px * ex + py * ey + pz * ez) * inv_len2;
+  t = fminf(fmaxf(t, 0.0f), 1.0f);
+  const float dx = px - t * ex, dy = py - t * ey, dz = pz - t * ez;
+  return dx * dx + dy * dy + dz * dz;
+}
+
+__device__ __forceinline__ float point_tri_dist2(float px, float py, float pz, const float4 &r0, const float4 &r1,
+                                                 const float4 &r2, const float4 &r3) {
+  const float ax = px - r0.x, ay = py - r0.y, az = pz - r0.z;  // ap
+  const float d_ab = seg_dist2(ax, ay, az, r1.x, r1.y, r1.z, r0.w);
+  const float d_ac = seg_dist2(ax, ay, az, r2.x, r2.y, r2.z, r1.w);
+  const float bx = ax - r1.x, by = ay - r1.y, bz = az - r1.z;  // bp
+  const float e3x = r2.x - r1.x, e3y = r2.y - r1.y, e3z = r2.z - r1.z;
+  const float d_bc = seg_dist2(bx, by, bz, e3x, e3y, e3z, r2.w);
+  // Barycentric tests against n: beta' = (ap x e2) . n, gamma' = (e1 x ap) . n
+  const float cx0 = ay * r2.z - az * r2.y, cy0 = az * r2.x - ax * r2.z, cz0 = ax * r2.y - ay * r2.x;
+  const float beta = cx0 * r3.x + cy0 * r3.y + cz0 * r3.z;
+  const float cx1 = r1.y * az - r1.z * ay, cy1 = r1.z * ax - r1.x * az, cz1 = r1.x * ay - r1.y * ax;
+  const float gamma = cx1 * r3.x + cy1 * r3.y + cz1 * r3.z;
+  const float h = ax * r3.x + ay * r3.y + az * r3.z;
+  const bool inside = (r3.w > 0.0f) & (beta >= 0.0f) & (gamma >= 0.0f) & ((beta + gamma) * r3.w <= 1.0f);
+  const float d_face = inside ? h * h * r3.w : __int_as_float(0x7f800000);
+  return fminf(fminf(d_face, d_ab), fminf(d_ac, d_bc));
+}
+
+// FP32 arithmetic of the routines above, counted as flops (add / sub / mul = 1, FMA = 2; min,
+// max and compares are not counted), for the roofline figure:
+// point_tri_dist2 = 3 (ap) + 3 x 17 (edge: dot 5, scale 1, p - t e 6, |.|^2 5) + 6 (bp, e3)
+//                 + 2 x 14 (cross 9 + dot 5) + 5 (h) + 2 (h^2 w) + 2 (inside test) = 97
+// box_dist2       = 3 x 2 (sub) + 5 (|d|^2) = 11
+constexpr int kFlopsPointTri = 97;
+constexpr int kFlopsPointBox = 11;
+
+// ---------------------------------------------------------------------------------------------
+// BVH node (64 bytes): the boxes of both children plus their references, so one 64-byte read
+// yields everything a traversal step needs.
+//   n0 = (c0.lo.x, c0.lo.y, c0.lo.z, c0.hi.x)
+//   n1 = (c0.hi.y, c0.hi.z, c1.lo.x, c1.lo.y)
+//   n2 = (c1.lo.z, c1.hi.x, c1.hi.y, c1.hi.z)
+//   n3 = (ref0, ref1, cnt0, cnt1) as ints: cnt == 0 -> ref is an inner node index;
+//        cnt > 0 -> leaf of cnt triangles starting at triangle record ref; cnt < 0 -> empty.
+struct Node {
+  float4 n0, n1, n2;
+  int4 n3;
+};
+
+__device__ __forceinline__ float box_dist2(float px, float py, float pz, float lx, float ly, float lz, float hx,
+                                           float hy, float hz) {
+  const float dx = fmaxf(fmaxf(lx - px, px - hx), 0.0f);
+  const float dy = fmaxf(fmaxf(ly - py, py - hy), 0.0f);
+  const float dz = fmaxf(fmaxf(lz - pz, pz - hz), 0.0f);
+  return dx * dx + dy * dy + dz * dz;
+}
+
+__device__ __forceinline__ void atomic_or_err(uint32_t *err, uint32_t bits) {
+  if (err) atomicOr(err, bits);
+}
+
+// Orderable float <-> uint mapping for atomic min / max of floats.
+__device__ __forceinline__ uint32_t float_to_ordered(float f) {
+  const uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__host__ __device__ __forceinline__ float ordered_to_float(uint32_t u) {
+  const uint32_t v = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(v);
+#else
+  float f;
+  __builtin_memcpy(&f, &v, 4);
+  return f;
+#endif
+}
+
+}  // namespace sdfb

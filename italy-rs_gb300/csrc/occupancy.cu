@@ -1,0 +1,166 @@
+// Dense occupancy: the reference's candidate-cell loop (src/convert/sdf_baker.cpp:89-118) as a
+// load-balanced expansion over (triangle, candidate cell) items.
+//
+// k_occ_items counts each triangle's clamped candidate box with the reference's FP32 rounding;
+// an exclusive scan turns the counts into item starts; k_occ_test takes chunks of items, runs the
+// exact-rounding SAT test (common.cuh) and stores 1 for hits. Several triangles may store 1 into
+// the same byte; the stores carry the same value, so no atomics are needed and the result does
+// not depend on their order.
+#include <algorithm>
+#include <cstdint>
+
+#include "common.cuh"
+#include "expand.cuh"
+#include "kernels.h"
+
+namespace sdfb {
+namespace {
+
+constexpr int kThreads = 256;
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct TriCells {
+  f3 a, b, c;
+  int lo[3], hi[3];
+};
+
+__device__ __forceinline__ f3 vload(const float *v, uint32_t i) {
+  return {__ldg(v + 3ull * i), __ldg(v + 3ull * i + 1), __ldg(v + 3ull * i + 2)};
+}
+
+// Out-of-range indices read vertex 0 (the bake reports the mesh as bad; reads stay in bounds).
+__device__ __forceinline__ TriCells tri_cells(const float *__restrict__ verts, const uint32_t *__restrict__ idx,
+                                              uint32_t V, uint32_t t, const GridDev &g) {
+  TriCells r;
+  const uint32_t i0 = __ldg(idx + 3ull * t), i1 = __ldg(idx + 3ull * t + 1), i2 = __ldg(idx + 3ull * t + 2);
+  r.a = vload(verts, i0 < V ? i0 : 0);
+  r.b = vload(verts, i1 < V ? i1 : 0);
+  r.c = vload(verts, i2 < V ? i2 : 0);
+  const float mn[3] = {min_ref(min_ref(r.a.x, r.b.x), r.c.x), min_ref(min_ref(r.a.y, r.b.y), r.c.y),
+                       min_ref(min_ref(r.a.z, r.b.z), r.c.z)};
+  const float mx[3] = {max_ref(max_ref(r.a.x, r.b.x), r.c.x), max_ref(max_ref(r.a.y, r.b.y), r.c.y),
+                       max_ref(max_ref(r.a.z, r.b.z), r.c.z)};
+  const float o[3] = {g.ox, g.oy, g.oz};
+  const int nmax[3] = {g.nx - 1, g.ny - 1, g.nz - 1};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    r.lo[k] = cell_index_clamped(mn[k], o[k], g.voxel, nmax[k]);
+    r.hi[k] = cell_index_clamped(mx[k], o[k], g.voxel, nmax[k]);
+  }
+  return r;
+}
+
+__global__ __launch_bounds__(kThreads) void k_occ_items(const float *__restrict__ verts,
+                                                        const uint32_t *__restrict__ idx, uint32_t V, uint32_t T, GridDev g,
+                                                        uint32_t *__restrict__ items) {
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  if (t >= T) return;
+  const TriCells tc = tri_cells(verts, idx, V, t, g);
+  const uint64_t n = uint64_t(tc.hi[0] - tc.lo[0] + 1) * uint64_t(tc.hi[1] - tc.lo[1] + 1) *
+                     uint64_t(tc.hi[2] - tc.lo[2] + 1);
+  items[t] = n > 0xffffffffull ? 0xffffffffu : static_cast<uint32_t>(n);
+}
+
+template <bool FIRST>
+__global__ __launch_bounds__(kThreads) void k_occ_test(const float *__restrict__ verts,
+                                                       const uint32_t *__restrict__ idx, uint32_t V, uint32_t T, GridDev g,
+                                                       const uint64_t *__restrict__ starts, uint8_t *__restrict__ occ,
+                                                       uint32_t *__restrict__ first_tri,
+                                                       unsigned long long *__restrict__ sat_tests) {
+  const uint64_t total = starts[T];
+  const uint64_t stride = uint64_t(gridDim.x) * kThreads * kExpandChunk;
+  const float h = __fmul_rn(g.voxel, 0.5f);
+  unsigned long long tests = 0;
+  for (uint64_t w0 = (uint64_t(blockIdx.x) * kThreads + threadIdx.x) * kExpandChunk; w0 < total; w0 += stride) {
+    uint32_t t = item_owner(starts, T, w0);
+    TriCells tc = tri_cells(verts, idx, V, t, g);
+    uint64_t tstart = starts[t], tend = starts[t + 1];
+    const uint64_t wend = min(w0 + kExpandChunk, total);
+    for (uint64_t w = w0; w < wend; ++w) {
+      while (w >= tend) {
+        ++t;
+        tstart = tend;
+        tend = starts[t + 1];
+        if (tend > tstart) tc = tri_cells(verts, idx, V, t, g);
+      }
+      const uint64_t k = w - tstart;
+      const uint32_t sx = tc.hi[0] - tc.lo[0] + 1, sy = tc.hi[1] - tc.lo[1] + 1;
+      const int x = tc.lo[0] + static_cast<int>(k % sx);
+      const int y = tc.lo[1] + static_cast<int>((k / sx) % sy);
+      const int z = tc.lo[2] + static_cast<int>(k / (uint64_t(sx) * sy));
+      const f3 c = {cell_center(g.ox, x, g.voxel), cell_center(g.oy, y, g.voxel), cell_center(g.oz, z, g.voxel)};
+      ++tests;
+      if (sat_overlap(c, h, tc.a, tc.b, tc.c)) {
+        const uint64_t cell = (uint64_t(z) * g.ny + y) * g.nx + x;
+        occ[cell] = 1;
+        if (FIRST) atomicMin(first_tri + cell, t);
+      }
+    }
+  }
+  if (sat_tests) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tests += __shfl_xor_sync(kFull, tests, o);
+    if ((threadIdx.x & 31) == 0 && tests) atomicAdd(sat_tests, tests);
+  }
+}
+
+struct OccTemp {
+  uint32_t *items;
+  uint64_t *starts;
+  void *scratch;
+  size_t scratch_bytes;
+};
+
+size_t occ_layout(uint32_t T, char *base, OccTemp *o) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char *p = base ? base + off : nullptr;
+    off += align256(bytes);
+    return p;
+  };
+  OccTemp x;
+  x.items = reinterpret_cast<uint32_t *>(take(size_t(T) * 4 + 4));
+  x.starts = reinterpret_cast<uint64_t *>(take((size_t(T) + 1) * 8));
+  x.scratch_bytes = scan_scratch_bytes(T);
+  x.scratch = take(x.scratch_bytes);
+  if (o) *o = x;
+  return off;
+}
+
+template <bool FIRST>
+cudaError_t occ_run(const float *verts, const uint32_t *idx, uint32_t V, uint32_t T, GridDev g, uint8_t *occ, uint32_t *first,
+                    void *temp, size_t temp_bytes, unsigned long long *sat_tests, cudaStream_t st) {
+  const size_t cells = size_t(g.nx) * g.ny * g.nz;
+  cudaError_t e = cudaMemsetAsync(occ, 0, cells, st);
+  if (e != cudaSuccess) return e;
+  if (FIRST && (e = cudaMemsetAsync(first, 0xff, cells * 4, st)) != cudaSuccess) return e;
+  if (T == 0) return cudaSuccess;
+  OccTemp o;
+  if (occ_layout(T, static_cast<char *>(temp), &o) > temp_bytes) return cudaErrorMemoryAllocation;
+  k_occ_items<<<(T + kThreads - 1) / kThreads, kThreads, 0, st>>>(verts, idx, V, T, g, o.items);
+  if ((e = exclusive_scan_u32(o.items, o.starts, T, Scratch{o.scratch, o.scratch_bytes}, st)) != cudaSuccess) return e;
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  k_occ_test<FIRST><<<sms * 8, kThreads, 0, st>>>(verts, idx, V, T, g, o.starts, occ, first, sat_tests);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t occupancy_temp_bytes(uint32_t num_tris) { return occ_layout(num_tris, nullptr, nullptr); }
+
+cudaError_t occupancy_dense(const float *verts, const uint32_t *idx, uint32_t num_verts, uint32_t num_tris, GridDev g,
+                            uint8_t *occ, void *temp, size_t temp_bytes, unsigned long long *sat_tests,
+                            cudaStream_t st) {
+  return occ_run<false>(verts, idx, num_verts, num_tris, g, occ, nullptr, temp, temp_bytes, sat_tests, st);
+}
+
+cudaError_t occupancy_dense_first(const float *verts, const uint32_t *idx, uint32_t num_verts, uint32_t num_tris,
+                                  GridDev g, uint8_t *occ, uint32_t *first_tri, void *temp, size_t temp_bytes,
+                                  cudaStream_t st) {
+  return occ_run<true>(verts, idx, num_verts, num_tris, g, occ, first_tri, temp, temp_bytes, nullptr, st);
+}
+
+}  // namespace sdfb

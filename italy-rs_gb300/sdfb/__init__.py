@@ -1,0 +1,299 @@
+"""ctypes binding of libsdfb.so, the GB300 mesh -> SDF bake (C ABI in include/sdfb.h).
+
+This is the Python face of the same entry points a C, C++ or FFI caller binds; tests and the
+benchmark go through it. Loading fails loudly when the library has not been built: there is no
+CPU fallback. Build it with ``python italy-rs_gb300/build.py`` (or ``__graft_entry__.build()``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(HERE), "lib", "libsdfb.so")
+
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_OUT_OF_MEMORY = 2
+ERR_CUDA = 3
+ERR_BAD_MESH = 4
+ERR_OVERFLOW = 5
+ERR_BUSY = 6
+ERR_TIMEOUT = 7
+ERR_NOT_FOUND = 8
+ERR_NO_DEVICE = 9
+ERR_INTERNAL = 10
+
+SIGN_AUTO, SIGN_PARITY, SIGN_GWN, SIGN_NONE = 0, 1, 2, 3
+
+
+class SdfbError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"sdfb status {status}: {message}")
+        self.status = status
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("voxel_size", C.c_float), ("nx", C.c_int32), ("ny", C.c_int32),
+                ("nz", C.c_int32)]
+
+    @property
+    def shape(self):
+        return (self.nz, self.ny, self.nx)
+
+    @property
+    def cells(self) -> int:
+        return int(self.nx) * int(self.ny) * int(self.nz)
+
+
+class Opts(C.Structure):
+    _fields_ = [("struct_size", C.c_uint32), ("sign_mode", C.c_int32), ("band_voxels", C.c_float),
+                ("leaf_size", C.c_int32), ("tile", C.c_int32), ("no_occupancy", C.c_int32),
+                ("no_distance", C.c_int32), ("count_work", C.c_int32), ("reserved", C.c_int32 * 8)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("struct_size", C.c_uint32), ("sign_mode_used", C.c_int32), ("watertight", C.c_int32),
+                ("leaf_size_used", C.c_int32), ("tile_used", C.c_int32), ("pad0", C.c_int32),
+                ("ms_total", C.c_double), ("ms_prepare", C.c_double), ("ms_build", C.c_double),
+                ("ms_occupancy", C.c_double), ("ms_sign", C.c_double), ("ms_distance", C.c_double),
+                ("voxels", C.c_uint64), ("triangles", C.c_uint64), ("sat_tests", C.c_uint64),
+                ("crossings", C.c_uint64), ("box_tests", C.c_uint64), ("tri_tests", C.c_uint64),
+                ("flops_distance", C.c_double), ("reserved", C.c_uint64 * 5)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "pad0", "struct_size")}
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("verts", C.c_void_p), ("idx", C.c_void_p), ("num_verts", C.c_uint32), ("num_tris", C.c_uint32)]
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("struct_size", C.c_uint32), ("hbm_budget_bytes", C.c_uint64), ("max_inflight", C.c_int32),
+                ("wave_voxels_log2", C.c_int32), ("reserved", C.c_int32 * 8)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("struct_size", C.c_uint32), ("status", C.c_int32), ("t_submit_ms", C.c_double),
+                ("t_admit_ms", C.c_double), ("t_done_ms", C.c_double), ("voxels", C.c_uint64),
+                ("mesh_was_resident", C.c_int32), ("pad", C.c_int32)]
+
+
+_P = C.c_void_p
+_u32, _i32, _u64 = C.c_uint32, C.c_int32, C.c_uint64
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "sdfb_abi_version": (_i32, []),
+    "sdfb_ctx_create": (_i32, [_i32, C.POINTER(_P)]),
+    "sdfb_ctx_destroy": (None, [_P]),
+    "sdfb_last_error": (C.c_char_p, [_P]),
+    "sdfb_ctx_trim": (_i32, [_P]),
+    "sdfb_ctx_device_bytes": (_u64, [_P]),
+    "sdfb_grid_from_bounds_res": (_i32, [_P, _P, _i32, C.POINTER(GridDesc)]),
+    "sdfb_bake": (_i32, [_P, _P, _u32, _P, _u32, C.POINTER(GridDesc), C.POINTER(Opts), _P, _P, C.POINTER(Stats)]),
+    "sdfb_bake_device": (_i32, [_P, _P, _u32, _P, _u32, C.POINTER(GridDesc), C.POINTER(Opts), _P, _P, _P,
+                                C.POINTER(Stats)]),
+    "sdfb_bake_soup": (_i32, [_P, _P, _u32, _P, _P, _i32, C.POINTER(Opts), C.POINTER(GridDesc), _P, _P,
+                              C.POINTER(Stats)]),
+    "sdfb_voxelize_sparse": (_i32, [_P, _P, _u32, _P, _P, _i32, _P, _u64, C.POINTER(_u64), _P, C.POINTER(C.c_float)]),
+    "sdfb_weld": (_i32, [_P, _P, _u32, _P, _P, _P, C.POINTER(_u32)]),
+    "sdfb_is_watertight": (_i32, [_P, _P, _u32, C.POINTER(_i32), C.POINTER(_u64), C.POINTER(_u64)]),
+    "sdfb_bake_batch": (_i32, [_P, _u32, C.POINTER(MeshDesc), C.POINTER(GridDesc), C.POINTER(Opts), _P, _P,
+                               C.POINTER(Stats)]),
+    "sdfb_bake_batch_device": (_i32, [_P, _u32, C.POINTER(MeshDesc), C.POINTER(GridDesc), C.POINTER(Opts), _P, _P,
+                                      _P, C.POINTER(Stats)]),
+    "sdfb_server_create": (_i32, [_P, C.POINTER(ServerOpts), C.POINTER(_P)]),
+    "sdfb_server_destroy": (None, [_P]),
+    "sdfb_mesh_register": (_i32, [_P, _P, _u32, _P, _u32, C.POINTER(_u64)]),
+    "sdfb_submit": (_i32, [_P, _u64, C.POINTER(GridDesc), C.POINTER(Opts), _P, _P, C.POINTER(_u64)]),
+    "sdfb_poll": (_i32, [_P, _u64, _i32, C.POINTER(_i32), C.POINTER(RequestInfo)]),
+    "sdfb_server_last_error": (C.c_char_p, [_P]),
+}
+
+_lib = None
+
+
+def load(path: str | None = None) -> C.CDLL:
+    """Loads libsdfb.so (raises if it is missing: there is no fallback)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise FileNotFoundError(f"{p} is not built; run italy-rs_gb300/build.py")
+    lib = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _u32a(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def make_grid(origin, voxel, n) -> GridDesc:
+    g = GridDesc()
+    for i in range(3):
+        g.origin[i] = float(origin[i])
+    g.voxel_size = float(np.float32(voxel))
+    g.nx, g.ny, g.nz = (int(x) for x in n)
+    return g
+
+
+def make_opts(sign_mode: int = SIGN_AUTO, band_voxels: float = 1.0, leaf_size: int = 0, tile: int = 0,
+              no_occupancy: bool = False, no_distance: bool = False, count_work: bool = False) -> Opts:
+    o = Opts()
+    o.struct_size = C.sizeof(Opts)
+    o.sign_mode = sign_mode
+    o.band_voxels = band_voxels
+    o.leaf_size = leaf_size
+    o.tile = tile
+    o.no_occupancy = int(no_occupancy)
+    o.no_distance = int(no_distance)
+    o.count_work = int(count_work)
+    return o
+
+
+def grid_from_bounds_res(bmin, bmax, resolution: int) -> GridDesc:
+    g = GridDesc()
+    st = load().sdfb_grid_from_bounds_res(_ptr(_f32(bmin)), _ptr(_f32(bmax)), int(resolution), C.byref(g))
+    if st != OK:
+        raise SdfbError(st, "grid too large")
+    return g
+
+
+def weld(positions, bmin, bmax):
+    p = _f32(positions).reshape(-1, 3)
+    out = np.empty(len(p), np.uint32)
+    n = C.c_uint32()
+    st = load().sdfb_weld(None, _ptr(p), len(p), _ptr(_f32(bmin)), _ptr(_f32(bmax)), _ptr(out), C.byref(n))
+    if st != OK:
+        raise SdfbError(st, "weld failed")
+    return out, int(n.value)
+
+
+def is_watertight(welded_idx):
+    w = _u32a(welded_idx).reshape(-1)
+    ok, b, m = C.c_int32(), C.c_uint64(), C.c_uint64()
+    st = load().sdfb_is_watertight(None, _ptr(w), len(w) // 3, C.byref(ok), C.byref(b), C.byref(m))
+    if st != OK:
+        raise SdfbError(st, "watertight test failed")
+    return bool(ok.value), int(b.value), int(m.value)
+
+
+class Context:
+    """One device context (streams, device memory, resident meshes)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        st = self.lib.sdfb_ctx_create(int(device), C.byref(h))
+        if st != OK:
+            raise SdfbError(st, "cannot create a context (no sm_103 device?)")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.sdfb_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def error(self) -> str:
+        return (self.lib.sdfb_last_error(self.h) or b"").decode()
+
+    def _check(self, st: int):
+        if st != OK:
+            raise SdfbError(st, self.error())
+
+    def bake(self, verts, idx, grid: GridDesc, opts: Opts | None = None, want_dist=True, want_occ=True,
+             stats: Stats | None = None):
+        """Host-buffer bake. Returns (dist float32[nz, ny, nx] or None, occ uint8[nz, ny, nx] or None)."""
+        v = _f32(verts).reshape(-1, 3)
+        i = _u32a(idx).reshape(-1, 3)
+        dist = np.empty(grid.shape, np.float32) if want_dist else None
+        occ = np.empty(grid.shape, np.uint8) if want_occ else None
+        st = self.lib.sdfb_bake(self.h, _ptr(v), len(v), _ptr(i), len(i), C.byref(grid),
+                                C.byref(opts) if opts is not None else None, _ptr(dist), _ptr(occ),
+                                C.byref(stats) if stats is not None else None)
+        self._check(st)
+        return dist, occ
+
+    def bake_status(self, verts, idx, grid: GridDesc, opts: Opts | None = None) -> tuple[int, str]:
+        """Runs a bake and returns (status, message) instead of raising (for error-path tests)."""
+        v = _f32(verts).reshape(-1, 3)
+        i = _u32a(idx).reshape(-1, 3)
+        dist = np.empty(grid.shape, np.float32)
+        occ = np.empty(grid.shape, np.uint8)
+        st = self.lib.sdfb_bake(self.h, _ptr(v), len(v), _ptr(i), len(i), C.byref(grid),
+                                C.byref(opts) if opts is not None else None, _ptr(dist), _ptr(occ), None)
+        return st, self.error()
+
+    def bake_device(self, d_verts: int, num_verts: int, d_idx: int, num_tris: int, grid: GridDesc,
+                    opts: Opts | None, d_dist: int, d_occ: int, stream: int = 0, stats: Stats | None = None):
+        st = self.lib.sdfb_bake_device(self.h, C.c_void_p(d_verts), num_verts, C.c_void_p(d_idx), num_tris,
+                                       C.byref(grid), C.byref(opts) if opts is not None else None,
+                                       C.c_void_p(d_dist), C.c_void_p(d_occ), C.c_void_p(stream),
+                                       C.byref(stats) if stats is not None else None)
+        self._check(st)
+
+    def bake_soup(self, positions, bmin, bmax, resolution: int, opts: Opts | None = None, stats: Stats | None = None):
+        p = _f32(positions).reshape(-1, 3)
+        g = GridDesc()
+        st = self.lib.sdfb_bake_soup(self.h, _ptr(p), len(p) // 3, _ptr(_f32(bmin)), _ptr(_f32(bmax)),
+                                     int(resolution), C.byref(opts) if opts is not None else None, C.byref(g), None,
+                                     None, None)
+        self._check(st)
+        dist = np.empty(g.shape, np.float32)
+        occ = np.empty(g.shape, np.uint8)
+        st = self.lib.sdfb_bake_soup(self.h, _ptr(p), len(p) // 3, _ptr(_f32(bmin)), _ptr(_f32(bmax)),
+                                     int(resolution), C.byref(opts) if opts is not None else None, C.byref(g),
+                                     _ptr(dist), _ptr(occ), C.byref(stats) if stats is not None else None)
+        self._check(st)
+        return g, dist, occ
+
+    def voxelize_sparse(self, positions, bmin, bmax, resolution: int):
+        p = _f32(positions).reshape(-1, 3)
+        cap = max(1024, 4 * len(p))
+        while True:
+            cells = np.empty((cap, 3), np.int32)
+            cnt = C.c_uint64()
+            o = np.zeros(3, np.float32)
+            v = C.c_float()
+            st = self.lib.sdfb_voxelize_sparse(self.h, _ptr(p), len(p) // 3, _ptr(_f32(bmin)), _ptr(_f32(bmax)),
+                                               int(resolution), _ptr(cells), cap, C.byref(cnt), _ptr(o), C.byref(v))
+            self._check(st)
+            if cnt.value <= cap:
+                return cells[:cnt.value].copy(), o, float(np.float32(v.value))
+            cap = int(cnt.value)
+
+    def device_bytes(self) -> int:
+        return int(self.lib.sdfb_ctx_device_bytes(self.h))
