@@ -102,7 +102,9 @@ typedef struct sdfb_stats {
   uint64_t box_tests;      /* point-box tests (lanes) when opts.count_work = 1 */
   uint64_t tri_tests;      /* point-triangle tests (lanes) when opts.count_work = 1 */
   double flops_distance;   /* FP32 flops of those tests (FMA = 2) */
-  uint64_t reserved[5];
+  uint64_t kernel_launches; /* kernels this call launched */
+  uint64_t gwn_fp64_cells;  /* GWN: cells whose winding number was evaluated in FP64 (band + ambiguous) */
+  uint64_t reserved[3];
 } sdfb_stats;
 
 /* ---- context ---------------------------------------------------------------------------- */

@@ -10,6 +10,7 @@
 // Replaces italy::bakeSdf (src/convert/sdf_baker.cpp:137-310), which builds an OptiX context,
 // GAS, module, pipeline and SBT on every call and copies the grid back synchronously.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -23,6 +24,12 @@
 #include "kernels.h"
 
 using namespace sdfb;
+
+namespace sdfb {
+static std::atomic<uint64_t> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
+}  // namespace sdfb
 
 // ---------------------------------------------------------------------------------------------
 // Context plumbing.
@@ -128,8 +135,10 @@ sdfb_status run_bake(sdfb_ctx *ctx, cudaStream_t st, const BakeInput &in, const 
   m.num_tris = T;
   m.verts = in.verts;
   m.idx = in.idx;
-  ENSURE(ctx->mesh, lbvh_mesh_bytes(T));
-  lbvh_bind_mesh(m, ctx->mesh.p);
+  const bool moments = want_dist && sign == kSignGwn;
+  ENSURE(ctx->mesh, lbvh_mesh_bytes(T, moments));
+  lbvh_bind_mesh(m, ctx->mesh.p, moments);
+  ctx->gwn_refined = 0;
   ENSURE(ctx->build_tmp, std::max(lbvh_temp_bytes(T), occupancy_temp_bytes(T)));
   ENSURE(ctx->misc, 256);
   uint32_t *d_err = static_cast<uint32_t *>(ctx->misc.p);
@@ -155,6 +164,7 @@ sdfb_status run_bake(sdfb_ctx *ctx, cudaStream_t st, const BakeInput &in, const 
     capacity = ctx->col_z.cap / 4;
   }
 
+  const uint64_t launches0 = launch_count();
   CK(cudaEventRecord(ctx->ev[0], st));
   CK(lbvh_build(m, leaf, ctx->build_tmp.p, ctx->build_tmp.cap, d_err, st));
   CK(cudaEventRecord(ctx->ev[1], st));
@@ -169,6 +179,8 @@ sdfb_status run_bake(sdfb_ctx *ctx, cudaStream_t st, const BakeInput &in, const 
   if (want_dist) {
     da.nodes = m.nodes;
     da.tris = m.tris;
+    da.num_nodes = static_cast<int>(std::max<uint32_t>(T, 2) - 1);
+    da.num_tris = static_cast<int>(T);
     da.g = g;
     da.sign = sign == kSignParity ? kSignParity : kSignNone;
     da.col_start = static_cast<const uint64_t *>(ctx->col_start.p);
@@ -197,6 +209,7 @@ sdfb_status run_bake(sdfb_ctx *ctx, cudaStream_t st, const BakeInput &in, const 
                     (h_err & kErrBadIndex) ? "triangle index out of range" : "mesh has a non-finite vertex");
   if (h_err & kErrStackOverflow)
     return ctx_fail(ctx, SDFB_ERR_OVERFLOW, "BVH traversal stack overflow (depth > 64)");
+  if (h_err & kErrCorruptTree) return ctx_fail(ctx, SDFB_ERR_INTERNAL, "BVH walk met an invalid reference");
   if (h_err & kErrCrossingOverflow) {
     // Rebuild the crossing list at its exact size, then rerun the distance pass.
     uint64_t need = 0;
@@ -240,6 +253,8 @@ sdfb_status run_bake(sdfb_ctx *ctx, cudaStream_t st, const BakeInput &in, const 
     s.tri_tests = w[1];
     s.sat_tests = w[2];
     s.flops_distance = double(w[0]) * kFlopsPointBox + double(w[1]) * kFlopsPointTri;
+    s.kernel_launches = launch_count() - launches0;
+    s.gwn_fp64_cells = ctx->gwn_refined;
     if (want_dist && sign == kSignParity)
       cudaMemcpy(&s.crossings, static_cast<uint64_t *>(ctx->col_start.p) + ncols, 8, cudaMemcpyDeviceToHost);
     const size_t n = std::min<size_t>(stats->struct_size ? stats->struct_size : sizeof s, sizeof s);

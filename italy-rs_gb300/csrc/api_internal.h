@@ -43,6 +43,7 @@ struct sdfb_ctx {
   // workspace of one bake
   DevBuf mesh, build_tmp, par_tmp, col_start, col_z, misc, gwn_tmp;
   uint64_t col_capacity_hint = 0;
+  uint64_t gwn_refined = 0;  // cells of the last bake that took the FP64 winding-number pass
 
   ~sdfb_ctx() {
     for (auto &e : ev)

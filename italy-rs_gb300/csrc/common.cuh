@@ -14,6 +14,7 @@ enum DevErr : uint32_t {
   kErrStackOverflow = 4u,     // traversal stack exhausted
   kErrCrossingOverflow = 8u,  // parity crossing list exceeded its capacity
   kErrEmpty = 16u,
+  kErrCorruptTree = 32u,      // a node or leaf reference out of range, or a walk that never ends
 };
 
 constexpr int kWarp = 32;

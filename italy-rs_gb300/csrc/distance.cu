@@ -42,7 +42,10 @@ __global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a, long long
   const int lx = lane % TX, ly = (lane / TX) % TY, lz = lane / kLayer;
   const GridDev g = a.g;
   unsigned long long box_tests = 0, tri_tests = 0;
-  bool overflow = false;
+  bool overflow = false, corrupt = false;
+  // A correct tree expands each inner node at most once per tile and pops at most once per
+  // push; anything longer means a corrupt tree, and the walk stops with an error.
+  const long long step_limit = 2ll * a.num_nodes + 64;
 
   for (;;) {
     long long tile = 0;
@@ -66,6 +69,10 @@ __global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a, long long
     }
 
     auto test_leaf = [&](int first, int count) {
+      if (first < 0 || count > a.num_tris - first) {
+        corrupt = true;
+        return;
+      }
       for (int k = 0; k < count; ++k) {
         const TriRec *tr = a.tris + first + k;
         const float4 r0 = __ldg(&tr->r0), r1 = __ldg(&tr->r1), r2 = __ldg(&tr->r2), r3 = __ldg(&tr->r3);
@@ -76,11 +83,19 @@ __global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a, long long
     };
 
     int cur = 0, sp = 0, stk0 = 0, stk1 = 0;
-    for (;;) {
+    for (long long steps = 0;; ++steps) {
+      if (steps > step_limit || (cur >= a.num_nodes)) {
+        corrupt = true;
+        break;
+      }
       if (cur < 0) {
         if (sp == 0) break;
         --sp;
         const int e = __shfl_sync(kFull, sp < 32 ? stk0 : stk1, sp & 31);
+        if ((e >> 1) >= a.num_nodes) {
+          corrupt = true;
+          break;
+        }
         const Node *np = a.nodes + (e >> 1);
         const float4 n0 = __ldg(&np->n0), n1 = __ldg(&np->n1), n2 = __ldg(&np->n2);
         const int4 n3 = __ldg(&np->n3);
@@ -186,6 +201,7 @@ __global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a, long long
     }
   }
   if (overflow) atomic_or_err(a.err, kErrStackOverflow);
+  if (corrupt) atomic_or_err(a.err, kErrCorruptTree);
   if (COUNT && a.work_counters && lane == 0) {
     atomicAdd(a.work_counters, box_tests);
     atomicAdd(a.work_counters + 1, tri_tests);
@@ -211,6 +227,7 @@ cudaError_t launch_shape(const DistanceArgs &a, int num_sms, cudaStream_t st) {
   if (e != cudaSuccess) return e;
   k_distance<s.tx, s.ty, s.tz, COUNT><<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(a, num_tiles, tiles_x,
                                                                                           tiles_y);
+  note_launch();
   return cudaGetLastError();
 }
 

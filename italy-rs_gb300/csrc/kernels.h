@@ -17,6 +17,11 @@ struct Scratch {
   size_t bytes = 0;
 };
 
+// Count of kernel launches issued by this library (every launcher calls note_launch once per
+// <<<...>>>); the bake reports the launches of one call in sdfb_stats.
+void note_launch();
+uint64_t launch_count();
+
 // ---- primitives.cu ----------------------------------------------------------------------------
 // Exclusive scan of n uint32 counts into uint64 starts; starts[n] receives the total, so `out`
 // must hold n + 1 values. Scratch need: scan_scratch_bytes(n).
@@ -39,14 +44,17 @@ struct MeshDev {
   Node *nodes = nullptr;            // max(T - 1, 1) nodes, root = 0
   uint32_t *leaf_order = nullptr;   // original triangle index of each record
   uint32_t *bounds = nullptr;       // 6 ordered-uint words: min xyz, max xyz
+  float4 *moments = nullptr;        // optional: 4 float4 per inner node (winding-number expansion)
   int leaf_size = 1;
 };
 
 // Temporaries of one build, sized by lbvh_temp_bytes(T).
 size_t lbvh_temp_bytes(uint32_t num_tris);
-size_t lbvh_mesh_bytes(uint32_t num_tris);  // tris + nodes + leaf_order + bounds
-// Carves a MeshDev's arrays out of `mem` (lbvh_mesh_bytes(T) bytes, 256-byte aligned).
-void lbvh_bind_mesh(MeshDev &m, void *mem);
+// tris + nodes + leaf_order + bounds (+ moments when with_moments)
+size_t lbvh_mesh_bytes(uint32_t num_tris, bool with_moments = false);
+// Carves a MeshDev's arrays out of `mem` (lbvh_mesh_bytes(T, with_moments) bytes, 256-aligned).
+void lbvh_bind_mesh(MeshDev &m, void *mem, bool with_moments = false);
+// Builds the hierarchy; when m.moments is set it also fills the winding-number moments.
 cudaError_t lbvh_build(MeshDev &m, int leaf_size, void *temp, size_t temp_bytes, uint32_t *err, cudaStream_t st);
 
 // ---- occupancy.cu -----------------------------------------------------------------------------
@@ -81,6 +89,8 @@ enum SignKind : int { kSignNone = 0, kSignParity = 1, kSignGwn = 2 };
 struct DistanceArgs {
   const Node *nodes;
   const TriRec *tris;
+  int num_nodes;  // inner nodes (max(T - 1, 1))
+  int num_tris;
   GridDev g;
   int sign;
   const uint64_t *col_start;  // parity

@@ -335,18 +335,119 @@ __global__ __launch_bounds__(kThreads) void k_gather(uint32_t T, const uint32_t 
   order[k] = t;
 }
 
+// Winding-number moments of every inner node, bottom-up like k_refit (Barill et al. 2018, "Fast
+// Winding Numbers for Soups and Clouds": each triangle is a dipole of area vector a = (e1 x e2)/2
+// at its centroid c; a node keeps N = sum a, P = area-weighted centroid, M = sum a (c - P)^T and
+// r = radius around P). Children combine as N = N0 + N1, P = (A0 P0 + A1 P1) / (A0 + A1),
+// M = M0 + N0 (P0 - P)^T + M1 + N1 (P1 - P)^T, r = max(r0 + |P0 - P|, r1 + |P1 - P|).
+struct Mom {
+  float px, py, pz, r, nx, ny, nz, area;
+  float m[9];
+};
+
+__device__ __forceinline__ Mom leaf_mom(const TriRec &t) {
+  Mom o;
+  const float cx = t.r0.x + (t.r1.x + t.r2.x) * (1.0f / 3.0f);
+  const float cy = t.r0.y + (t.r1.y + t.r2.y) * (1.0f / 3.0f);
+  const float cz = t.r0.z + (t.r1.z + t.r2.z) * (1.0f / 3.0f);
+  o.px = cx;
+  o.py = cy;
+  o.pz = cz;
+  o.nx = 0.5f * t.r3.x;
+  o.ny = 0.5f * t.r3.y;
+  o.nz = 0.5f * t.r3.z;
+  o.area = sqrtf(o.nx * o.nx + o.ny * o.ny + o.nz * o.nz);
+  const float ax = t.r0.x - cx, ay = t.r0.y - cy, az = t.r0.z - cz;
+  const float bx = ax + t.r1.x, by = ay + t.r1.y, bz = az + t.r1.z;
+  const float qx = ax + t.r2.x, qy = ay + t.r2.y, qz = az + t.r2.z;
+  o.r = sqrtf(fmaxf(fmaxf(ax * ax + ay * ay + az * az, bx * bx + by * by + bz * bz), qx * qx + qy * qy + qz * qz));
+#pragma unroll
+  for (int k = 0; k < 9; ++k) o.m[k] = 0.0f;
+  return o;
+}
+
+__device__ __forceinline__ Mom combine(const Mom &a, const Mom &b) {
+  Mom o;
+  const float A = a.area + b.area;
+  const float wa = A > 0.0f ? a.area / A : 0.5f, wb = 1.0f - wa;
+  o.px = wa * a.px + wb * b.px;
+  o.py = wa * a.py + wb * b.py;
+  o.pz = wa * a.pz + wb * b.pz;
+  o.area = A;
+  o.nx = a.nx + b.nx;
+  o.ny = a.ny + b.ny;
+  o.nz = a.nz + b.nz;
+  const float da[3] = {a.px - o.px, a.py - o.py, a.pz - o.pz}, db[3] = {b.px - o.px, b.py - o.py, b.pz - o.pz};
+  const float na[3] = {a.nx, a.ny, a.nz}, nb[3] = {b.nx, b.ny, b.nz};
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) o.m[3 * i + j] = a.m[3 * i + j] + b.m[3 * i + j] + na[i] * da[j] + nb[i] * db[j];
+  o.r = fmaxf(a.r + sqrtf(da[0] * da[0] + da[1] * da[1] + da[2] * da[2]),
+              b.r + sqrtf(db[0] * db[0] + db[1] * db[1] + db[2] * db[2]));
+  return o;
+}
+
+__device__ __forceinline__ void store_mom(float4 *mom, float *area, int i, const Mom &o) {
+  __stcg(mom + 4 * i + 0, make_float4(o.px, o.py, o.pz, o.r));
+  __stcg(mom + 4 * i + 1, make_float4(o.nx, o.ny, o.nz, o.m[0]));
+  __stcg(mom + 4 * i + 2, make_float4(o.m[1], o.m[2], o.m[3], o.m[4]));
+  __stcg(mom + 4 * i + 3, make_float4(o.m[5], o.m[6], o.m[7], o.m[8]));
+  __stcg(area + i, o.area);
+}
+
+__device__ __forceinline__ Mom load_mom(const float4 *mom, const float *area, int i) {
+  Mom o;
+  const float4 a = __ldcg(mom + 4 * i), b = __ldcg(mom + 4 * i + 1), c = __ldcg(mom + 4 * i + 2),
+               d = __ldcg(mom + 4 * i + 3);
+  o.px = a.x; o.py = a.y; o.pz = a.z; o.r = a.w;
+  o.nx = b.x; o.ny = b.y; o.nz = b.z; o.m[0] = b.w;
+  o.m[1] = c.x; o.m[2] = c.y; o.m[3] = c.z; o.m[4] = c.w;
+  o.m[5] = d.x; o.m[6] = d.y; o.m[7] = d.z; o.m[8] = d.w;
+  o.area = __ldcg(area + i);
+  return o;
+}
+
+__global__ __launch_bounds__(kThreads) void k_moments(int n, const TriRec *__restrict__ tris,
+                                                      const int2 *__restrict__ child, const int *__restrict__ iparent,
+                                                      const int *__restrict__ lparent, int *visits, float4 *mom,
+                                                      float *area) {
+  const int leaf = blockIdx.x * kThreads + threadIdx.x;
+  if (leaf >= n) return;
+  int node = lparent[leaf];
+  while (node >= 0) {
+    __threadfence();
+    if (atomicAdd(visits + node, 1) == 0) return;
+    __threadfence();
+    const int2 c = child[node];
+    const Mom a = c.x < 0 ? leaf_mom(tris[c.x & 0x7fffffff]) : load_mom(mom, area, c.x);
+    const Mom b = c.y < 0 ? leaf_mom(tris[c.y & 0x7fffffff]) : load_mom(mom, area, c.y);
+    store_mom(mom, area, node, combine(a, b));
+    node = iparent[node];
+  }
+}
+
+__global__ void k_moments_single(const TriRec *tris, float4 *mom) {
+  const Mom o = leaf_mom(tris[0]);
+  mom[0] = make_float4(o.px, o.py, o.pz, o.r);
+  mom[1] = make_float4(o.nx, o.ny, o.nz, 0.0f);
+  mom[2] = make_float4(0, 0, 0, 0);
+  mom[3] = make_float4(0, 0, 0, 0);
+}
+
 inline unsigned blocks_for(size_t n) { return static_cast<unsigned>((n + kThreads - 1) / kThreads); }
 
 }  // namespace
 
 size_t lbvh_temp_bytes(uint32_t num_tris) { return temp_layout(num_tris, nullptr, nullptr); }
 
-size_t lbvh_mesh_bytes(uint32_t T) {
+size_t lbvh_mesh_bytes(uint32_t T, bool with_moments) {
   const size_t n = std::max<uint32_t>(T, 1), m = std::max<uint32_t>(T, 2) - 1;
-  return align256(n * sizeof(TriRec)) + align256(m * sizeof(Node)) + align256(n * 4) + align256(6 * 4);
+  return align256(n * sizeof(TriRec)) + align256(m * sizeof(Node)) + align256(n * 4) + align256(6 * 4) +
+         (with_moments ? align256(m * 4 * sizeof(float4)) : 0);
 }
 
-void lbvh_bind_mesh(MeshDev &m, void *mem) {
+void lbvh_bind_mesh(MeshDev &m, void *mem, bool with_moments) {
   const size_t n = std::max<uint32_t>(m.num_tris, 1), k = std::max<uint32_t>(m.num_tris, 2) - 1;
   char *p = static_cast<char *>(mem);
   m.tris = reinterpret_cast<TriRec *>(p);
@@ -356,6 +457,8 @@ void lbvh_bind_mesh(MeshDev &m, void *mem) {
   m.leaf_order = reinterpret_cast<uint32_t *>(p);
   p += align256(n * 4);
   m.bounds = reinterpret_cast<uint32_t *>(p);
+  p += align256(6 * 4);
+  m.moments = with_moments ? reinterpret_cast<float4 *>(p) : nullptr;
 }
 
 cudaError_t lbvh_build(MeshDev &m, int leaf_size, void *temp, size_t temp_bytes, uint32_t *err, cudaStream_t st) {
@@ -368,25 +471,45 @@ cudaError_t lbvh_build(MeshDev &m, int leaf_size, void *temp, size_t temp_bytes,
   m.leaf_size = leaf_size;
   cudaError_t e;
   k_init_bounds<<<1, 32, 0, st>>>(m.bounds);
+  note_launch();
   k_prep<<<blocks_for(T), kThreads, 0, st>>>(m.verts, m.idx, m.num_verts, T, t.rec, t.lo, t.hi, m.bounds, err);
+  note_launch();
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (T == 1) {
     k_single<<<1, 1, 0, st>>>(t.lo, t.hi, m.nodes);
+    note_launch();
     k_gather<<<1, kThreads, 0, st>>>(1, nullptr, t.rec, m.tris, m.leaf_order);
+    note_launch();
+    if (m.moments) {
+      k_moments_single<<<1, 1, 0, st>>>(m.tris, m.moments);
+      note_launch();
+    }
     return cudaGetLastError();
   }
   k_morton<<<blocks_for(T), kThreads, 0, st>>>(t.lo, t.hi, T, m.bounds, t.keys, t.vals);
+  note_launch();
   if ((e = radix_sort_pairs(t.keys, t.vals, t.keys_alt, t.vals_alt, T, 30, Scratch{t.scratch, t.scratch_bytes}, st)) !=
       cudaSuccess)
     return e;
   const int n = static_cast<int>(T);
   k_hierarchy<<<blocks_for(T - 1), kThreads, 0, st>>>(t.keys, n, t.child, t.range, t.iparent, t.lparent);
+  note_launch();
   if ((e = cudaMemsetAsync(t.visits, 0, sizeof(int) * (T - 1), st)) != cudaSuccess) return e;
   k_refit<<<blocks_for(T), kThreads, 0, st>>>(n, t.vals, t.lo, t.hi, t.child, t.iparent, t.lparent, t.visits, t.ilo,
                                                t.ihi);
+  note_launch();
   k_layout<<<blocks_for(T - 1), kThreads, 0, st>>>(n, leaf_size, t.vals, t.lo, t.hi, t.child, t.range, t.ilo, t.ihi,
                                                     m.nodes);
+  note_launch();
   k_gather<<<blocks_for(T), kThreads, 0, st>>>(T, t.vals, t.rec, m.tris, m.leaf_order);
+  note_launch();
+  if (m.moments) {
+    // the inner boxes are no longer needed: their space holds the node areas
+    if ((e = cudaMemsetAsync(t.visits, 0, sizeof(int) * (T - 1), st)) != cudaSuccess) return e;
+    k_moments<<<blocks_for(T), kThreads, 0, st>>>(n, m.tris, t.child, t.iparent, t.lparent, t.visits, m.moments,
+                                                  reinterpret_cast<float *>(t.ilo));
+    note_launch();
+  }
   return cudaGetLastError();
 }
 

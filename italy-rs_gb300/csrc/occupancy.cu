@@ -139,11 +139,13 @@ cudaError_t occ_run(const float *verts, const uint32_t *idx, uint32_t V, uint32_
   OccTemp o;
   if (occ_layout(T, static_cast<char *>(temp), &o) > temp_bytes) return cudaErrorMemoryAllocation;
   k_occ_items<<<(T + kThreads - 1) / kThreads, kThreads, 0, st>>>(verts, idx, V, T, g, o.items);
+  note_launch();
   if ((e = exclusive_scan_u32(o.items, o.starts, T, Scratch{o.scratch, o.scratch_bytes}, st)) != cudaSuccess) return e;
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   k_occ_test<FIRST><<<sms * 8, kThreads, 0, st>>>(verts, idx, V, T, g, o.starts, occ, first, sat_tests);
+  note_launch();
   return cudaGetLastError();
 }
 

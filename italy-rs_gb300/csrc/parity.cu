@@ -158,16 +158,19 @@ cudaError_t parity_columns(const float *verts, const uint32_t *idx, uint32_t V, 
   if (T == 0) return cudaMemsetAsync(col_start, 0, (ncols + 1) * 8, st);
   const Scratch sc{o.scratch, o.scratch_bytes};
   k_col_items<<<(T + kThreads - 1) / kThreads, kThreads, 0, st>>>(verts, idx, V, T, g, o.items);
+  note_launch();
   if ((e = exclusive_scan_u32(o.items, o.starts, T, sc, st)) != cudaSuccess) return e;
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const unsigned grid = sms * 8;
   k_col_hits<false><<<grid, kThreads, 0, st>>>(verts, idx, V, T, g, o.starts, o.col_count, nullptr, nullptr, 0, err);
+  note_launch();
   if ((e = exclusive_scan_u32(o.col_count, col_start, ncols, sc, st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(o.col_count, 0, ncols * 4, st)) != cudaSuccess) return e;
   k_col_hits<true><<<grid, kThreads, 0, st>>>(verts, idx, V, T, g, o.starts, o.col_count, col_start, col_z, capacity,
                                               err);
+  note_launch();
   return cudaGetLastError();
 }
 

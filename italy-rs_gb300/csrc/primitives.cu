@@ -104,16 +104,19 @@ cudaError_t scan_impl(const Tin *in, uint64_t *out, size_t n, Bump &b, cudaStrea
   const size_t ntiles = (n + kScanTile - 1) / kScanTile;
   if (ntiles == 1) {
     k_scan_tiles<Tin><<<1, kScanThreads, 0, st>>>(in, out, nullptr, n);
+    note_launch();
     return cudaGetLastError();
   }
   uint64_t *sums = b.take<uint64_t>(ntiles);
   uint64_t *offs = b.take<uint64_t>(ntiles + 1);
   if (!sums || !offs) return cudaErrorMemoryAllocation;
   k_scan_tiles<Tin><<<static_cast<unsigned>(ntiles), kScanThreads, 0, st>>>(in, out, sums, n);
+  note_launch();
   cudaError_t e = scan_impl<uint64_t>(sums, offs, ntiles, b, st);
   if (e != cudaSuccess) return e;
   const unsigned blocks = static_cast<unsigned>(std::min<size_t>((n + 255) / 256, 4096));
   k_add_tile_offsets<<<blocks, 256, 0, st>>>(out, offs, n, ntiles);
+  note_launch();
   return cudaGetLastError();
 }
 
@@ -220,10 +223,12 @@ cudaError_t radix_sort_pairs(uint64_t *keys, uint32_t *vals, uint64_t *keys_alt,
   int passes = 0;
   for (int shift = 0; shift < bits; shift += 8, ++passes) {
     k_sort_hist<<<static_cast<unsigned>(ntiles), kSortThreads, 0, st>>>(ka, n, shift, hist, ntiles);
+    note_launch();
     Bump bs = b;
     cudaError_t e = scan_impl<uint32_t>(hist, offs, cells, bs, st);
     if (e != cudaSuccess) return e;
     k_sort_scatter<<<static_cast<unsigned>(ntiles), kSortThreads, 0, st>>>(ka, va, kb, vb, n, shift, offs, ntiles);
+    note_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     std::swap(ka, kb);
     std::swap(va, vb);

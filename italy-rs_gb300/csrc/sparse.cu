@@ -111,6 +111,7 @@ cudaError_t sparse_count(const uint8_t *occ, size_t cells, void *temp, size_t te
   if (sparse_layout(cells, 0, static_cast<char *>(temp), &o) > temp_bytes) return cudaErrorMemoryAllocation;
   const size_t tiles = (cells + kTile - 1) / kTile;
   k_tile_count<<<static_cast<unsigned>(tiles), kThreads, 0, st>>>(occ, cells, o.counts);
+  note_launch();
   cudaError_t e = exclusive_scan_u32(o.counts, o.starts, tiles, Scratch{o.scratch, o.scratch_bytes}, st);
   if (e != cudaSuccess) return e;
   if ((e = cudaMemcpyAsync(h_total, o.starts + tiles, 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
@@ -125,6 +126,7 @@ cudaError_t sparse_emit(const uint8_t *occ, const uint32_t *first_tri, size_t ce
   if (sparse_layout(cells, total, static_cast<char *>(temp), &o) > temp_bytes) return cudaErrorMemoryAllocation;
   const size_t tiles = (cells + kTile - 1) / kTile;
   k_tile_write<<<static_cast<unsigned>(tiles), kThreads, 0, st>>>(occ, first_tri, cells, o.starts, o.keys, cells_out);
+  note_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   return radix_sort_pairs(o.keys, cells_out, o.keys_alt, o.vals_alt, total, tri_bits,

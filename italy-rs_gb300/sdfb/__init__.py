@@ -61,7 +61,8 @@ class Stats(C.Structure):
                 ("ms_occupancy", C.c_double), ("ms_sign", C.c_double), ("ms_distance", C.c_double),
                 ("voxels", C.c_uint64), ("triangles", C.c_uint64), ("sat_tests", C.c_uint64),
                 ("crossings", C.c_uint64), ("box_tests", C.c_uint64), ("tri_tests", C.c_uint64),
-                ("flops_distance", C.c_double), ("reserved", C.c_uint64 * 5)]
+                ("flops_distance", C.c_double), ("kernel_launches", C.c_uint64), ("gwn_fp64_cells", C.c_uint64),
+                ("reserved", C.c_uint64 * 3)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "pad0", "struct_size")}

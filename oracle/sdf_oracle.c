@@ -499,6 +499,13 @@ static double point_tri_dist2(const double *p, const dtri *t) {
     ab[i] = b[i] - a[i]; ac[i] = c[i] - a[i];
     ap[i] = p[i] - a[i]; bp[i] = p[i] - b[i]; cp[i] = p[i] - c[i];
   }
+  /* A zero-area triangle (collinear or coincident vertices) is the union of its edges; the region
+   * walk below would divide by zero on a zero-length edge. */
+  const double nx = ab[1] * ac[2] - ab[2] * ac[1], ny = ab[2] * ac[0] - ab[0] * ac[2], nz = ab[0] * ac[1] - ab[1] * ac[0];
+  if (!(nx * nx + ny * ny + nz * nz > 1e-30 * dot3(ab, ab) * dot3(ac, ac))) {
+    const double e0 = seg_dist2(p, a, b), e1 = seg_dist2(p, b, c), e2 = seg_dist2(p, c, a);
+    return fmin(e0, fmin(e1, e2));
+  }
   const double d1 = dot3(ab, ap), d2 = dot3(ac, ap);
   if (d1 <= 0.0 && d2 <= 0.0) return dot3(ap, ap);
   const double d3 = dot3(ab, bp), d4 = dot3(ac, bp);

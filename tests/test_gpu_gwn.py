@@ -1,0 +1,73 @@
+"""Winding-number sign on meshes with holes (needs an sm_103 device).
+
+The oracle sums every triangle's solid angle in FP64; the bake's sign must equal |w| > 0.5 for
+every cell farther than one voxel from the surface whose oracle winding number is not within
+1e-6 of 0.5 (such cells sit on the w = 0.5 level set and have no robust sign)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+DIST_TOL = 1e-5
+
+
+def holey_soup(seed: int, sphere_level=3, torus=(48, 16), fraction=0.05):
+    from sdfb import meshgen as mg
+    rng = np.random.default_rng(seed)
+    parts = [mg.displaced_icosphere(sphere_level, 0.22, int(rng.integers(1 << 30)), center=(-0.15, 0.05, 0.0)),
+             mg.displaced_torus(torus[0], torus[1], 0.2, 0.07, int(rng.integers(1 << 30)), center=(0.18, -0.1, 0.05))]
+    v, f = mg.concat(parts)
+    return mg.delete_faces(v, f, fraction, int(rng.integers(1 << 30)))
+
+
+@pytest.mark.parametrize("seed,n", [(3, 40), (4, 56)])
+def test_gwn_sign_matches_fp64_oracle(ctx, oracle, seed, n):
+    import sdfb
+    v, f = holey_soup(seed)
+    origin, voxel = (-0.5,) * 3, 1.0 / n
+    grid = sdfb.make_grid(origin, voxel, (n, n, n))
+    st = sdfb.Stats()
+    st.struct_size = sdfb.C.sizeof(sdfb.Stats)
+    dist, occ = ctx.bake(v, f, grid, sdfb.make_opts(sign_mode=sdfb.SIGN_AUTO), stats=st)
+    assert st.watertight == 0 and st.sign_mode_used == sdfb.SIGN_GWN
+    assert st.gwn_fp64_cells > 0
+    flat = dist.reshape(-1)
+    d64 = oracle.distance(v, f, origin, voxel, (n, n, n))
+    assert np.abs(np.abs(flat.astype(np.float64)) - d64).max() <= DIST_TOL * np.sqrt(3)
+    assert np.array_equal(occ.reshape(-1), oracle.occupancy(v, f, origin, voxel, (n, n, n)))
+    w = oracle.gwn(v, f, origin, voxel, (n, n, n))
+    far = (d64 > voxel) & (np.abs(np.abs(w) - 0.5) > 1e-6)
+    bad = np.count_nonzero((flat[far] < 0) != (np.abs(w[far]) > 0.5))
+    assert bad == 0, f"{bad} winding-number sign mismatches outside the band"
+    # in the band the FP64 pass decides; report, and require near-total agreement
+    near = (d64 <= voxel) & (np.abs(np.abs(w) - 0.5) > 1e-6)
+    bad_near = np.count_nonzero((flat[near] < 0) != (np.abs(w[near]) > 0.5))
+    assert bad_near <= max(2, near.sum() // 1000)
+
+
+def test_gwn_equals_parity_on_closed_mesh(ctx):
+    import sdfb
+    from sdfb import meshgen as mg
+    v, f = mg.displaced_icosphere(4, 0.33, 21)
+    grid = sdfb.make_grid((-0.5,) * 3, 1.0 / 64, (64, 64, 64))
+    dp, _ = ctx.bake(v, f, grid, sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY))
+    dg, _ = ctx.bake(v, f, grid, sdfb.make_opts(sign_mode=sdfb.SIGN_GWN))
+    assert np.array_equal(np.abs(dp), np.abs(dg))
+    far = np.abs(dp) > 1.0 / 64
+    assert np.array_equal(dp[far] < 0, dg[far] < 0)
+    near = ~far
+    assert np.count_nonzero((dp[near] < 0) != (dg[near] < 0)) <= 2
+
+
+def test_gwn_band_width_option(ctx):
+    import sdfb
+    v, f = holey_soup(7)
+    grid = sdfb.make_grid((-0.5,) * 3, 1.0 / 40, (40, 40, 40))
+    s1, s3 = sdfb.Stats(), sdfb.Stats()
+    s1.struct_size = s3.struct_size = sdfb.C.sizeof(sdfb.Stats)
+    d1, _ = ctx.bake(v, f, grid, sdfb.make_opts(sign_mode=sdfb.SIGN_GWN, band_voxels=1.0), stats=s1)
+    d3, _ = ctx.bake(v, f, grid, sdfb.make_opts(sign_mode=sdfb.SIGN_GWN, band_voxels=3.0), stats=s3)
+    assert s3.gwn_fp64_cells > s1.gwn_fp64_cells
+    assert np.array_equal(np.abs(d1), np.abs(d3))

@@ -184,3 +184,27 @@ def test_oracle_matches_live_reference_occupancy(reference, oracle):
         cr, _, _ = reference.voxelize(tri, lo, hi, res)
         co, _, _ = oracle.voxelize_sparse(tri, lo, hi, res)
         assert np.array_equal(cr, co)
+
+
+def test_degenerate_triangles_are_their_edges(oracle):
+    """Zero-area triangles (collinear, two coincident vertices, a point) measure as the union of
+    their edges."""
+    v = np.array([[0, 0, 0], [0.2, 0.1, 0.0], [0.4, 0.2, 0.0], [0.1, 0.3, 0.2], [0.1, 0.3, 0.2]], np.float32)
+    i = np.array([[0, 1, 2], [3, 4, 0], [2, 2, 2]], np.uint32)
+    n = (12, 12, 12)
+    o = np.float32(-0.2)
+    vox = np.float32(0.05)
+    d = oracle.distance(v, i, (o,) * 3, vox, n)
+    c = (o + (np.arange(12, dtype=np.float32) + np.float32(0.5)) * vox).astype(np.float32)
+    Z, Y, X = np.meshgrid(c, c, c, indexing="ij")
+    P = np.stack([X, Y, Z], -1).reshape(-1, 3).astype(np.float64)
+
+    def seg(a, b):
+        ab = b - a
+        l2 = ab @ ab
+        t = np.clip(((P - a) @ ab) / l2, 0, 1) if l2 > 0 else np.zeros(len(P))
+        return np.linalg.norm(P - a - t[:, None] * ab, axis=1)
+
+    V = v.astype(np.float64)
+    bf = np.minimum.reduce([seg(V[0], V[2]), seg(V[3], V[0]), seg(V[2], V[2])])
+    assert np.abs(bf - d).max() < 1e-12
