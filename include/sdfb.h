@@ -73,11 +73,13 @@ typedef struct sdfb_opts {
   int32_t sign_mode;      /* sdfb_sign_mode, default AUTO */
   float band_voxels;      /* GWN: width in voxels of the FP64 band around the surface, default 1 */
   int32_t leaf_size;      /* BVH leaf size 1..16, default: autotuned table */
-  int32_t tile;           /* distance tile shape id (see sdfb_tile_count), default: autotuned */
+  int32_t tile;           /* distance tile shape 1..6 (4x4x2, 8x4x1, 4x4x4, 8x4x2, 4x4x8, 8x4x4
+                             cells per warp), 0: autotuned table */
   int32_t no_occupancy;   /* 1: skip occupancy (occ_out may be NULL) */
   int32_t no_distance;    /* 1: occupancy only (dist_out may be NULL) */
   int32_t count_work;     /* 1: count traversal work into stats (a slower, instrumented kernel) */
-  int32_t reserved[8];
+  int32_t stack_depth;    /* traversal stack entries, 32 or 64, 0: autotuned table */
+  int32_t reserved[7];
 } sdfb_opts;
 
 /* Per-call statistics, filled when the pointer is non-null. Times are CUDA-event times on the
@@ -88,7 +90,7 @@ typedef struct sdfb_stats {
   int32_t watertight;      /* 1, 0, or -1 when not evaluated */
   int32_t leaf_size_used;
   int32_t tile_used;
-  int32_t pad0;
+  int32_t stack_used;
   double ms_total;         /* first to last event on the device */
   double ms_prepare;       /* validation, triangle layout, bounds */
   double ms_build;         /* Morton codes, sort, hierarchy, refit */
@@ -104,7 +106,8 @@ typedef struct sdfb_stats {
   double flops_distance;   /* FP32 flops of those tests (FMA = 2) */
   uint64_t kernel_launches; /* kernels this call launched */
   uint64_t gwn_fp64_cells;  /* GWN: cells whose winding number was evaluated in FP64 (band + ambiguous) */
-  uint64_t reserved[3];
+  uint64_t graph_replayed;  /* 1 when the launch sequence was replayed from a CUDA graph */
+  uint64_t reserved[2];
 } sdfb_stats;
 
 /* ---- context ---------------------------------------------------------------------------- */
@@ -170,6 +173,28 @@ sdfb_status sdfb_weld(sdfb_ctx *ctx, const float *positions, uint32_t num_positi
  * used once (boundary) or more than twice (non-manifold); degenerate triangles are skipped. */
 sdfb_status sdfb_is_watertight(sdfb_ctx *ctx, const uint32_t *welded_idx, uint32_t num_tris, int32_t *watertight,
                                uint64_t *boundary_edges, uint64_t *nonmanifold_edges);
+
+/* ---- batched bake -------------------------------------------------------------------------- */
+
+typedef struct sdfb_mesh_desc {
+  const float *verts;    /* V x 3 */
+  const uint32_t *idx;   /* T x 3 */
+  uint32_t num_verts;
+  uint32_t num_tris;
+} sdfb_mesh_desc;
+
+/* Bakes `count` meshes, each onto its own grid, in one persistent launch per stage replayed from
+ * a CUDA graph. Buffers are host memory; dist_outs[i] / occ_outs[i] have grid i's cell count
+ * (either array, or any entry, may be NULL). stats (optional) receives the aggregate. */
+sdfb_status sdfb_bake_batch(sdfb_ctx *ctx, uint32_t count, const sdfb_mesh_desc *meshes,
+                            const sdfb_grid_desc *grids, const sdfb_opts *opts, float *const *dist_outs,
+                            uint8_t *const *occ_outs, sdfb_stats *stats);
+
+/* Device-buffer form of the batched bake: every pointer in meshes/dist_outs/occ_outs is device
+ * memory. Returns after completion. */
+sdfb_status sdfb_bake_batch_device(sdfb_ctx *ctx, uint32_t count, const sdfb_mesh_desc *meshes,
+                                   const sdfb_grid_desc *grids, const sdfb_opts *opts, float *const *dist_outs,
+                                   uint8_t *const *occ_outs, void *stream, sdfb_stats *stats);
 
 #ifdef __cplusplus
 }

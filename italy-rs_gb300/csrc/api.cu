@@ -1,14 +1,11 @@
-// C ABI of the bake (include/sdfb.h): context, device workspace, and the plain single-mesh bake.
+// C ABI of the bake (include/sdfb.h): context, buffers and every entry point. Each entry point
+// resolves sign modes on the host (the reference's weld + watertight gate,
+// src/io/mesh_weld.cpp:26-48 and src/io/mesh_validate.cpp:21-59), caps non-watertight meshes for
+// the winding number, places inputs and outputs in device memory and hands the meshes to
+// run_batch (orchestrate.cu).
 //
-// One bake on a stream (run_bake): reset the error word -> build the BVH (lbvh.cu) -> occupancy
-// (occupancy.cu) -> parity crossing lists (parity.cu) or winding-number signs (gwn.cu) ->
-// distance with fused sign (distance.cu). CUDA events bracket each stage for the per-stage
-// times in sdfb_stats. After the stream drains, the device error word is read: bad indices and
-// non-finite vertices become SDFB_ERR_BAD_MESH; a crossing list that outgrew its buffer is rebuilt
-// once at its exact size.
-//
-// Replaces italy::bakeSdf (src/convert/sdf_baker.cpp:137-310), which builds an OptiX context,
-// GAS, module, pipeline and SBT on every call and copies the grid back synchronously.
+// Replaces italy::bakeSdf (src/convert/sdf_baker.cpp:137-310) and italy::voxelizeMesh
+// (src/convert/voxelize.cpp:52-107).
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -32,7 +29,7 @@ uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 }  // namespace sdfb
 
 // ---------------------------------------------------------------------------------------------
-// Context plumbing.
+// Buffers, errors, context.
 
 bool DevBuf::ensure(size_t bytes) {
   if (bytes <= cap) return true;
@@ -53,6 +50,56 @@ void DevBuf::release() {
   cap = 0;
 }
 
+bool PinBuf::ensure(size_t bytes) {
+  if (bytes <= cap) return true;
+  release();
+  const size_t want = std::max<size_t>(bytes + bytes / 8, 4096);
+  if (cudaMallocHost(&p, want) != cudaSuccess) {
+    cudaGetLastError();
+    p = nullptr;
+    return false;
+  }
+  cap = want;
+  return true;
+}
+
+void PinBuf::release() {
+  if (p) cudaFreeHost(p);
+  p = nullptr;
+  cap = 0;
+}
+
+sdfb_ctx::~sdfb_ctx() {
+  if (graph) cudaGraphExecDestroy(graph);
+  for (auto &e : ev)
+    if (e) cudaEventDestroy(e);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+DevBuf *sdfb_ctx::all_bufs(int i) {
+  DevBuf *b[] = {&in_verts, &in_idx,    &in_verts2, &in_idx2,   &in_caps,  &in_capidx, &out_dist,
+                 &out_occ,  &first_tri, &batch_buf, &bvh,       &build_tmp, &par_tmp,  &col_start,
+                 &col_z,    &col_s,     &caps_bvh,  &caps_tmp,  &misc,     &gwn_tmp};
+  return i < int(sizeof b / sizeof b[0]) ? b[i] : nullptr;
+}
+
+void sdfb_ctx::release_all() {
+  if (graph) {
+    cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    graph_key.clear();
+  }
+  for (int i = 0; DevBuf *b = all_bufs(i); ++i) b->release();
+  staging.release();
+  staging_out.release();
+}
+
+uint64_t sdfb_ctx::device_bytes() const {
+  uint64_t s = 0;
+  for (int i = 0; const DevBuf *b = const_cast<sdfb_ctx *>(this)->all_bufs(i); ++i) s += b->cap;
+  return s;
+}
+
 sdfb_status ctx_fail(sdfb_ctx *ctx, sdfb_status st, const char *fmt, ...) {
   char buf[512];
   va_list ap;
@@ -69,10 +116,10 @@ sdfb_status ctx_cuda(sdfb_ctx *ctx, cudaError_t e, const char *what) {
   return ctx_fail(ctx, SDFB_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
-#define CK(call)                                                  \
-  do {                                                            \
-    const cudaError_t e_ = (call);                                \
-    if (e_ != cudaSuccess) return ctx_cuda(ctx, e_, #call);       \
+#define CK(call)                                            \
+  do {                                                      \
+    const cudaError_t e_ = (call);                          \
+    if (e_ != cudaSuccess) return ctx_cuda(ctx, e_, #call); \
   } while (0)
 
 #define ENSURE(buf, bytes)                                                                       \
@@ -96,13 +143,6 @@ GridDev to_dev(const sdfb_grid_desc &g) {
   return GridDev{g.origin[0], g.origin[1], g.origin[2], g.voxel_size, g.nx, g.ny, g.nz};
 }
 
-void default_params(uint32_t T, uint64_t cells, int *leaf, int *tile) {
-  (void)T;
-  (void)cells;
-  *leaf = 4;
-  *tile = 2;
-}
-
 sdfb_opts opts_or_default(const sdfb_opts *o) {
   sdfb_opts r;
   std::memset(&r, 0, sizeof r);
@@ -113,170 +153,65 @@ sdfb_opts opts_or_default(const sdfb_opts *o) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// One bake on device buffers.
+// Host-side preparation.
 
-sdfb_status run_bake(sdfb_ctx *ctx, cudaStream_t st, const BakeInput &in, const sdfb_grid_desc &grid,
-                     const sdfb_opts &opts, int sign, float *d_dist, uint8_t *d_occ, sdfb_stats *stats) {
-  const uint32_t T = in.num_tris;
-  const GridDev g = to_dev(grid);
-  const uint64_t cells = uint64_t(grid.nx) * grid.ny * grid.nz;
-  int leaf = opts.leaf_size, tile = opts.tile;
-  int dleaf, dtile;
-  default_params(T, cells, &dleaf, &dtile);
-  if (leaf <= 0) leaf = dleaf;
-  if (tile <= 0 || tile >= tile_shape_count()) tile = (opts.tile == 0) ? dtile : 0;
-  leaf = std::max(1, std::min(leaf, 16));
-  const bool want_dist = d_dist && !opts.no_distance;
-  const bool want_occ = d_occ && !opts.no_occupancy;
+namespace {
 
-  // Workspace.
-  MeshDev m;
-  m.num_verts = in.num_verts;
-  m.num_tris = T;
-  m.verts = in.verts;
-  m.idx = in.idx;
-  const bool moments = want_dist && sign == kSignGwn;
-  ENSURE(ctx->mesh, lbvh_mesh_bytes(T, moments));
-  lbvh_bind_mesh(m, ctx->mesh.p, moments);
-  ctx->gwn_refined = 0;
-  ENSURE(ctx->build_tmp, std::max(lbvh_temp_bytes(T), occupancy_temp_bytes(T)));
-  ENSURE(ctx->misc, 256);
-  uint32_t *d_err = static_cast<uint32_t *>(ctx->misc.p);
-  unsigned long long *d_tile = reinterpret_cast<unsigned long long *>(static_cast<char *>(ctx->misc.p) + 64);
-  unsigned long long *d_work = reinterpret_cast<unsigned long long *>(static_cast<char *>(ctx->misc.p) + 128);
-  unsigned long long *d_sat = reinterpret_cast<unsigned long long *>(static_cast<char *>(ctx->misc.p) + 160);
-  CK(cudaMemsetAsync(ctx->misc.p, 0, 256, st));
-
-  const size_t ncols = size_t(grid.nx) * grid.ny;
-  BakeInput pin = in;  // the mesh whose crossings decide parity (the welded mesh for soups)
-  if (in.parity_verts) {
-    pin.verts = in.parity_verts;
-    pin.idx = in.parity_idx;
-    pin.num_verts = in.parity_num_verts;
-    pin.num_tris = in.parity_num_tris;
-  }
-  uint64_t capacity = 0;
-  if (want_dist && sign == kSignParity) {
-    ENSURE(ctx->par_tmp, parity_temp_bytes(pin.num_tris, grid.nx, grid.ny));
-    ENSURE(ctx->col_start, (ncols + 1) * 8);
-    capacity = std::max<uint64_t>(ctx->col_capacity_hint, std::max<uint64_t>(4 * ncols, 2 * uint64_t(pin.num_tris)));
-    ENSURE(ctx->col_z, capacity * 4);
-    capacity = ctx->col_z.cap / 4;
-  }
-
-  const uint64_t launches0 = launch_count();
-  CK(cudaEventRecord(ctx->ev[0], st));
-  CK(lbvh_build(m, leaf, ctx->build_tmp.p, ctx->build_tmp.cap, d_err, st));
-  CK(cudaEventRecord(ctx->ev[1], st));
-  if (want_occ)
-    CK(occupancy_dense(in.verts, in.idx, in.num_verts, T, g, d_occ, ctx->build_tmp.p, ctx->build_tmp.cap, d_sat, st));
-  CK(cudaEventRecord(ctx->ev[2], st));
-  if (want_dist && sign == kSignParity)
-    CK(parity_columns(pin.verts, pin.idx, pin.num_verts, pin.num_tris, g, static_cast<uint64_t *>(ctx->col_start.p),
-                      static_cast<float *>(ctx->col_z.p), capacity, ctx->par_tmp.p, ctx->par_tmp.cap, d_err, st));
-  CK(cudaEventRecord(ctx->ev[3], st));
-  DistanceArgs da{};
-  if (want_dist) {
-    da.nodes = m.nodes;
-    da.tris = m.tris;
-    da.num_nodes = static_cast<int>(std::max<uint32_t>(T, 2) - 1);
-    da.num_tris = static_cast<int>(T);
-    da.g = g;
-    da.sign = sign == kSignParity ? kSignParity : kSignNone;
-    da.col_start = static_cast<const uint64_t *>(ctx->col_start.p);
-    da.col_z = static_cast<const float *>(ctx->col_z.p);
-    da.dist = d_dist;
-    da.err = d_err;
-    da.tile_counter = d_tile;
-    da.work_counters = opts.count_work ? d_work : nullptr;
-  }
-  CK(cudaEventRecord(ctx->ev[4], st));
-  if (want_dist) CK(distance_launch(da, tile, ctx->num_sms, st));
-  if (want_dist && sign == kSignGwn) {
-    CK(cudaEventRecord(ctx->ev[6], st));
-    const sdfb_status gs = gwn_apply(ctx, st, m, in, grid, opts, d_dist, d_err);
-    if (gs != SDFB_OK) return gs;
-  } else {
-    CK(cudaEventRecord(ctx->ev[6], st));
-  }
-  CK(cudaEventRecord(ctx->ev[5], st));
-
-  uint32_t h_err = 0;
-  CK(cudaMemcpyAsync(&h_err, d_err, 4, cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
-  if (h_err & (kErrBadIndex | kErrNonFinite))
-    return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "%s",
-                    (h_err & kErrBadIndex) ? "triangle index out of range" : "mesh has a non-finite vertex");
-  if (h_err & kErrStackOverflow)
-    return ctx_fail(ctx, SDFB_ERR_OVERFLOW, "BVH traversal stack overflow (depth > 64)");
-  if (h_err & kErrCorruptTree) return ctx_fail(ctx, SDFB_ERR_INTERNAL, "BVH walk met an invalid reference");
-  if (h_err & kErrCrossingOverflow) {
-    // Rebuild the crossing list at its exact size, then rerun the distance pass.
-    uint64_t need = 0;
-    CK(cudaMemcpy(&need, static_cast<uint64_t *>(ctx->col_start.p) + ncols, 8, cudaMemcpyDeviceToHost));
-    ctx->col_capacity_hint = need + need / 4;
-    ENSURE(ctx->col_z, ctx->col_capacity_hint * 4);
-    capacity = ctx->col_z.cap / 4;
-    CK(cudaMemsetAsync(d_err, 0, 4, st));
-    CK(parity_columns(pin.verts, pin.idx, pin.num_verts, pin.num_tris, g, static_cast<uint64_t *>(ctx->col_start.p),
-                      static_cast<float *>(ctx->col_z.p), capacity, ctx->par_tmp.p, ctx->par_tmp.cap, d_err, st));
-    da.col_z = static_cast<const float *>(ctx->col_z.p);
-    CK(distance_launch(da, tile, ctx->num_sms, st));
-    CK(cudaMemcpyAsync(&h_err, d_err, 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    if (h_err) return ctx_fail(ctx, SDFB_ERR_INTERNAL, "crossing list overflow after resize");
-  }
-
-  if (stats) {
-    sdfb_stats s;
-    std::memset(&s, 0, sizeof s);
-    s.struct_size = sizeof s;
-    s.sign_mode_used = sign == kSignParity ? SDFB_SIGN_PARITY : (sign == kSignGwn ? SDFB_SIGN_GWN : SDFB_SIGN_NONE);
-    s.watertight = in.watertight;
-    s.leaf_size_used = leaf;
-    s.tile_used = tile;
-    float ms[4], ms_dist = 0, ms_gwn = 0, tot = 0;
-    for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&ms[i], ctx->ev[i], ctx->ev[i + 1]);
-    cudaEventElapsedTime(&ms_dist, ctx->ev[4], ctx->ev[6]);
-    cudaEventElapsedTime(&ms_gwn, ctx->ev[6], ctx->ev[5]);
-    cudaEventElapsedTime(&tot, ctx->ev[0], ctx->ev[5]);
-    s.ms_total = tot;
-    s.ms_build = ms[0];
-    s.ms_occupancy = ms[1];
-    s.ms_sign = ms[2] + ms[3] + ms_gwn;
-    s.ms_distance = ms_dist;
-    s.voxels = cells;
-    s.triangles = T;
-    unsigned long long w[4] = {0, 0, 0, 0};
-    cudaMemcpy(w, d_work, 32, cudaMemcpyDeviceToHost);
-    s.box_tests = w[0];
-    s.tri_tests = w[1];
-    s.sat_tests = w[2];
-    s.flops_distance = double(w[0]) * kFlopsPointBox + double(w[1]) * kFlopsPointTri;
-    s.kernel_launches = launch_count() - launches0;
-    s.gwn_fp64_cells = ctx->gwn_refined;
-    if (want_dist && sign == kSignParity)
-      cudaMemcpy(&s.crossings, static_cast<uint64_t *>(ctx->col_start.p) + ncols, 8, cudaMemcpyDeviceToHost);
-    const size_t n = std::min<size_t>(stats->struct_size ? stats->struct_size : sizeof s, sizeof s);
-    std::memcpy(stats, &s, n);
-  }
-  return SDFB_OK;
-}
-
-// Resolves AUTO: welds the mesh and runs the watertight test on the host copy.
-int resolve_sign(const sdfb_opts &o, const float *h_verts, uint32_t V, const uint32_t *h_idx, uint32_t T,
-                 int *watertight_out) {
-  *watertight_out = -1;
+// Sign of one mesh from the options and, for AUTO, the watertight gate on the host copy.
+// Returns -1 when an index is out of range (AUTO only).
+int resolve_sign(const sdfb_opts &o, const float *hv, uint32_t V, const uint32_t *hi, uint32_t T, int *watertight) {
+  *watertight = -1;
   switch (o.sign_mode) {
     case SDFB_SIGN_PARITY: return kSignParity;
     case SDFB_SIGN_GWN: return kSignGwn;
     case SDFB_SIGN_NONE: return kSignNone;
     default: break;
   }
-  const int w = indexed_mesh_watertight(h_verts, V, h_idx, T);
-  *watertight_out = w == 1 ? 1 : 0;
+  const int w = indexed_mesh_watertight(hv, V, hi, T);
+  if (w == -2) return -1;
+  *watertight = w == 1 ? 1 : 0;
   return w == 1 ? kSignParity : kSignGwn;
 }
+
+sdfb_status upload_caps(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &ms, std::vector<CapBuild> &caps) {
+  size_t nv = 0, np = 0, nc = 0;
+  for (size_t m = 0; m < ms.size(); ++m)
+    if (ms[m].sign == kSignGwn) {
+      nv += caps[m].verts.size();
+      np += caps[m].pidx.size();
+      nc += caps[m].cidx.size();
+    }
+  if (nv == 0) return SDFB_OK;
+  ENSURE(ctx->in_caps, nv * 4);
+  ENSURE(ctx->in_idx2, np * 4);
+  ENSURE(ctx->in_capidx, std::max<size_t>(nc, 1) * 4);
+  size_t ov = 0, op = 0, oc = 0;
+  for (size_t m = 0; m < ms.size(); ++m) {
+    if (ms[m].sign != kSignGwn) continue;
+    const CapBuild &c = caps[m];
+    float *dv = static_cast<float *>(ctx->in_caps.p) + ov;
+    uint32_t *dp = static_cast<uint32_t *>(ctx->in_idx2.p) + op;
+    uint32_t *dc = static_cast<uint32_t *>(ctx->in_capidx.p) + oc;
+    CK(cudaMemcpyAsync(dv, c.verts.data(), c.verts.size() * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dp, c.pidx.data(), c.pidx.size() * 4, cudaMemcpyHostToDevice, st));
+    if (!c.cidx.empty()) CK(cudaMemcpyAsync(dc, c.cidx.data(), c.cidx.size() * 4, cudaMemcpyHostToDevice, st));
+    ms[m].pverts = dv;
+    ms[m].pidx = dp;
+    ms[m].pV = static_cast<uint32_t>(c.verts.size() / 3);
+    ms[m].pT = static_cast<uint32_t>(c.pidx.size() / 3);
+    ms[m].cverts = dv;
+    ms[m].cidx = dc;
+    ms[m].cT = static_cast<uint32_t>(c.cidx.size() / 3);
+    ov += c.verts.size();
+    op += c.pidx.size();
+    oc += c.cidx.size();
+  }
+  // the caps arrays are host vectors read by asynchronous copies: wait before they go away
+  CK(cudaStreamSynchronize(st));
+  return SDFB_OK;
+}
+
+}  // namespace
 
 // ---------------------------------------------------------------------------------------------
 // C ABI.
@@ -311,6 +246,7 @@ sdfb_status sdfb_ctx_create(int32_t device, sdfb_ctx **out) {
       delete ctx;
       return SDFB_ERR_CUDA;
     }
+  load_tuning(ctx);
   *out = ctx;
   return SDFB_OK;
 }
@@ -372,20 +308,38 @@ sdfb_status sdfb_bake_device(sdfb_ctx *ctx, const float *d_verts, uint32_t num_v
   cudaSetDevice(ctx->device);
   const sdfb_opts o = opts_or_default(opts);
   cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
-  int watertight = -1;
-  int sign;
-  if (o.sign_mode == SDFB_SIGN_AUTO) {
+  std::vector<PlanMesh> ms(1);
+  PlanMesh &p = ms[0];
+  p.verts = d_verts;
+  p.idx = d_idx;
+  p.V = num_verts;
+  p.T = num_tris;
+  p.grid = *grid;
+  p.dist = o.no_distance ? nullptr : d_dist_out;
+  p.occ = o.no_occupancy ? nullptr : d_occ_out;
+  std::vector<CapBuild> caps(1);
+  if (o.sign_mode == SDFB_SIGN_AUTO || o.sign_mode == SDFB_SIGN_GWN) {
+    // the watertight gate and the caps need the mesh on the host
     std::vector<float> hv(size_t(num_verts) * 3);
     std::vector<uint32_t> hi(size_t(num_tris) * 3);
     CK(cudaMemcpyAsync(hv.data(), d_verts, hv.size() * 4, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(hi.data(), d_idx, hi.size() * 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    sign = resolve_sign(o, hv.data(), num_verts, hi.data(), num_tris, &watertight);
+    p.sign = resolve_sign(o, hv.data(), num_verts, hi.data(), num_tris, &p.watertight);
+    if (p.sign < 0) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "triangle index out of range");
+    if (p.sign == kSignGwn && p.dist) {
+      for (size_t k = 0; k < hi.size(); ++k)
+        if (hi[k] >= num_verts) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "triangle index out of range");
+      build_caps(hv.data(), num_verts, hi.data(), num_tris, caps[0]);
+    }
   } else {
-    sign = resolve_sign(o, nullptr, 0, nullptr, 0, &watertight);
+    p.sign = resolve_sign(o, nullptr, 0, nullptr, 0, &p.watertight);
   }
-  BakeInput in{d_verts, d_idx, num_verts, num_tris, nullptr, nullptr, 0, 0, watertight};
-  return run_bake(ctx, st, in, *grid, o, sign, d_dist_out, d_occ_out, stats);
+  if (p.sign == kSignGwn && p.dist) {
+    const sdfb_status s = upload_caps(ctx, st, ms, caps);
+    if (s != SDFB_OK) return s;
+  }
+  return run_batch(ctx, st, ms, o, false, stats);
 }
 
 sdfb_status sdfb_bake(sdfb_ctx *ctx, const float *verts, uint32_t num_verts, const uint32_t *idx, uint32_t num_tris,
@@ -398,23 +352,37 @@ sdfb_status sdfb_bake(sdfb_ctx *ctx, const float *verts, uint32_t num_verts, con
   if (num_tris == 0 || num_verts == 0) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh has no triangles");
   cudaSetDevice(ctx->device);
   const sdfb_opts o = opts_or_default(opts);
-  int watertight = -1;
-  const int sign = resolve_sign(o, verts, num_verts, idx, num_tris, &watertight);
-  if (watertight == -1 && o.sign_mode == SDFB_SIGN_AUTO)
-    return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "triangle index out of range");
   const cudaStream_t st = ctx->stream;
+  std::vector<PlanMesh> ms(1);
+  PlanMesh &p = ms[0];
+  p.sign = resolve_sign(o, verts, num_verts, idx, num_tris, &p.watertight);
+  if (p.sign < 0) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "triangle index out of range");
   const uint64_t cells = uint64_t(grid->nx) * grid->ny * grid->nz;
+  const bool want_dist = dist_out && !o.no_distance, want_occ = occ_out && !o.no_occupancy;
+  std::vector<CapBuild> caps(1);
+  if (p.sign == kSignGwn && want_dist) {
+    for (size_t k = 0; k < size_t(num_tris) * 3; ++k)
+      if (idx[k] >= num_verts) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "triangle index out of range");
+    build_caps(verts, num_verts, idx, num_tris, caps[0]);
+  }
   ENSURE(ctx->in_verts, size_t(num_verts) * 12);
   ENSURE(ctx->in_idx, size_t(num_tris) * 12);
-  const bool want_dist = dist_out && !o.no_distance, want_occ = occ_out && !o.no_occupancy;
   if (want_dist) ENSURE(ctx->out_dist, cells * 4);
   if (want_occ) ENSURE(ctx->out_occ, cells);
   CK(cudaMemcpyAsync(ctx->in_verts.p, verts, size_t(num_verts) * 12, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(ctx->in_idx.p, idx, size_t(num_tris) * 12, cudaMemcpyHostToDevice, st));
-  BakeInput in{static_cast<const float *>(ctx->in_verts.p), static_cast<const uint32_t *>(ctx->in_idx.p), num_verts,
-               num_tris, nullptr, nullptr, 0, 0, watertight};
-  sdfb_status s = run_bake(ctx, st, in, *grid, o, sign, want_dist ? static_cast<float *>(ctx->out_dist.p) : nullptr,
-                           want_occ ? static_cast<uint8_t *>(ctx->out_occ.p) : nullptr, stats);
+  p.verts = static_cast<const float *>(ctx->in_verts.p);
+  p.idx = static_cast<const uint32_t *>(ctx->in_idx.p);
+  p.V = num_verts;
+  p.T = num_tris;
+  p.grid = *grid;
+  p.dist = want_dist ? static_cast<float *>(ctx->out_dist.p) : nullptr;
+  p.occ = want_occ ? static_cast<uint8_t *>(ctx->out_occ.p) : nullptr;
+  if (p.sign == kSignGwn && want_dist) {
+    const sdfb_status s = upload_caps(ctx, st, ms, caps);
+    if (s != SDFB_OK) return s;
+  }
+  const sdfb_status s = run_batch(ctx, st, ms, o, false, stats);
   if (s != SDFB_OK) return s;
   if (want_dist) CK(cudaMemcpyAsync(dist_out, ctx->out_dist.p, cells * 4, cudaMemcpyDeviceToHost, st));
   if (want_occ) CK(cudaMemcpyAsync(occ_out, ctx->out_occ.p, cells, cudaMemcpyDeviceToHost, st));
@@ -435,9 +403,9 @@ sdfb_status sdfb_bake_soup(sdfb_ctx *ctx, const float *positions, uint32_t num_t
   if (!grid_ok(grid_out)) return ctx_fail(ctx, SDFB_ERR_INVALID_ARGUMENT, "grid too large");
   if (num_tris == 0) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh has no triangles");
   cudaSetDevice(ctx->device);
-  sdfb_opts o = opts_or_default(opts);
+  const sdfb_opts o = opts_or_default(opts);
   const uint32_t V = 3 * num_tris;
-  // Weld for the watertight gate and for a crack-free parity mesh (first occurrence kept).
+  // Weld (first occurrence kept) for the watertight gate and for a crack-free crossing mesh.
   std::vector<uint32_t> welded(V);
   const uint32_t U = weld_positions(positions, V, bounds_min, bounds_max, welded.data());
   std::vector<float> uniq(size_t(U) * 3);
@@ -447,41 +415,48 @@ sdfb_status sdfb_bake_soup(sdfb_ctx *ctx, const float *positions, uint32_t num_t
       seen[welded[i]] = 1;
       std::memcpy(&uniq[size_t(welded[i]) * 3], positions + size_t(i) * 3, 12);
     }
-  int watertight = -1;
-  int sign;
+  std::vector<PlanMesh> ms(1);
+  PlanMesh &p = ms[0];
   if (o.sign_mode == SDFB_SIGN_AUTO) {
     uint64_t b, m;
-    watertight = watertight_flag(welded.data(), num_tris, &b, &m);
-    sign = watertight == 1 ? kSignParity : kSignGwn;
+    p.watertight = watertight_flag(welded.data(), num_tris, &b, &m) == 1 ? 1 : 0;
+    p.sign = p.watertight ? kSignParity : kSignGwn;
   } else {
-    sign = resolve_sign(o, nullptr, 0, nullptr, 0, &watertight);
+    p.sign = resolve_sign(o, nullptr, 0, nullptr, 0, &p.watertight);
   }
   std::vector<uint32_t> ident(V);
   for (uint32_t i = 0; i < V; ++i) ident[i] = i;
   const cudaStream_t st = ctx->stream;
   const uint64_t cells = uint64_t(grid_out->nx) * grid_out->ny * grid_out->nz;
+  const bool want_dist = dist_out && !o.no_distance, want_occ = occ_out && !o.no_occupancy;
   ENSURE(ctx->in_verts, size_t(V) * 12);
   ENSURE(ctx->in_idx, size_t(V) * 4);
-  ENSURE(ctx->in_verts2, size_t(U) * 12);
-  ENSURE(ctx->in_idx2, size_t(V) * 4);
-  const bool want_dist = dist_out && !o.no_distance, want_occ = occ_out && !o.no_occupancy;
   if (want_dist) ENSURE(ctx->out_dist, cells * 4);
   if (want_occ) ENSURE(ctx->out_occ, cells);
   CK(cudaMemcpyAsync(ctx->in_verts.p, positions, size_t(V) * 12, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(ctx->in_idx.p, ident.data(), size_t(V) * 4, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(ctx->in_verts2.p, uniq.data(), size_t(U) * 12, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(ctx->in_idx2.p, welded.data(), size_t(V) * 4, cudaMemcpyHostToDevice, st));
-  BakeInput in{static_cast<const float *>(ctx->in_verts.p),
-               static_cast<const uint32_t *>(ctx->in_idx.p),
-               V,
-               num_tris,
-               static_cast<const float *>(ctx->in_verts2.p),
-               static_cast<const uint32_t *>(ctx->in_idx2.p),
-               U,
-               num_tris,
-               watertight};
-  s = run_bake(ctx, st, in, *grid_out, o, sign, want_dist ? static_cast<float *>(ctx->out_dist.p) : nullptr,
-               want_occ ? static_cast<uint8_t *>(ctx->out_occ.p) : nullptr, stats);
+  p.verts = static_cast<const float *>(ctx->in_verts.p);
+  p.idx = static_cast<const uint32_t *>(ctx->in_idx.p);
+  p.V = V;
+  p.T = num_tris;
+  p.grid = *grid_out;
+  p.dist = want_dist ? static_cast<float *>(ctx->out_dist.p) : nullptr;
+  p.occ = want_occ ? static_cast<uint8_t *>(ctx->out_occ.p) : nullptr;
+  if (p.sign == kSignGwn && want_dist) {
+    std::vector<CapBuild> caps(1);
+    build_caps(uniq.data(), U, welded.data(), num_tris, caps[0]);
+    if ((s = upload_caps(ctx, st, ms, caps)) != SDFB_OK) return s;
+  } else if (p.sign == kSignParity && want_dist) {
+    ENSURE(ctx->in_verts2, size_t(U) * 12);
+    ENSURE(ctx->in_idx2, size_t(V) * 4);
+    CK(cudaMemcpyAsync(ctx->in_verts2.p, uniq.data(), size_t(U) * 12, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->in_idx2.p, welded.data(), size_t(V) * 4, cudaMemcpyHostToDevice, st));
+    p.pverts = static_cast<const float *>(ctx->in_verts2.p);
+    p.pidx = static_cast<const uint32_t *>(ctx->in_idx2.p);
+    p.pV = U;
+    p.pT = num_tris;
+  }
+  s = run_batch(ctx, st, ms, o, false, stats);
   if (s != SDFB_OK) return s;
   if (want_dist) CK(cudaMemcpyAsync(dist_out, ctx->out_dist.p, cells * 4, cudaMemcpyDeviceToHost, st));
   if (want_occ) CK(cudaMemcpyAsync(occ_out, ctx->out_occ.p, cells, cudaMemcpyDeviceToHost, st));
@@ -548,9 +523,38 @@ sdfb_status sdfb_voxelize_sparse(sdfb_ctx *ctx, const float *positions, uint32_t
   ENSURE(ctx->build_tmp, occupancy_temp_bytes(num_tris));
   CK(cudaMemcpyAsync(ctx->in_verts.p, positions, size_t(V) * 12, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(ctx->in_idx.p, ident.data(), size_t(V) * 4, cudaMemcpyHostToDevice, st));
-  CK(occupancy_dense_first(static_cast<const float *>(ctx->in_verts.p), static_cast<const uint32_t *>(ctx->in_idx.p),
-                           V, num_tris, to_dev(g), static_cast<uint8_t *>(ctx->out_occ.p),
-                           static_cast<uint32_t *>(ctx->first_tri.p), ctx->build_tmp.p, ctx->build_tmp.cap, st));
+  // a batch of one mesh with an occupancy output only
+  MeshRec r;
+  std::memset(&r, 0, sizeof r);
+  r.verts = static_cast<const float *>(ctx->in_verts.p);
+  r.idx = static_cast<const uint32_t *>(ctx->in_idx.p);
+  r.num_verts = V;
+  r.num_tris = num_tris;
+  r.occ = static_cast<uint8_t *>(ctx->out_occ.p);
+  r.g = to_dev(g);
+  r.leaf_size = 1;
+  const uint64_t tables[2][2] = {{0, num_tris}, {0, cells}};
+  const uint64_t zero[2] = {0, 0};
+  const size_t bytes = 256 * 4;
+  ENSURE(ctx->batch_buf, bytes);
+  if (!ctx->staging.ensure(bytes)) return ctx_fail(ctx, SDFB_ERR_OUT_OF_MEMORY, "pinned staging");
+  char *hs = static_cast<char *>(ctx->staging.p);
+  std::memcpy(hs, &r, sizeof r);
+  std::memcpy(hs + 256, tables[0], 16);
+  std::memcpy(hs + 512, tables[1], 16);
+  std::memcpy(hs + 768, zero, 16);
+  CK(cudaMemcpyAsync(ctx->batch_buf.p, hs, bytes, cudaMemcpyHostToDevice, st));
+  char *d = static_cast<char *>(ctx->batch_buf.p);
+  BatchDev B;
+  B.num_meshes = 1;
+  B.recs = reinterpret_cast<const MeshRec *>(d);
+  B.tri_starts = reinterpret_cast<const uint64_t *>(d + 256);
+  B.cell_starts = reinterpret_cast<const uint64_t *>(d + 512);
+  B.ptri_starts = B.tile_starts = B.gwn_tile_starts = reinterpret_cast<const uint64_t *>(d + 768);
+  B.total_tris = num_tris;
+  B.total_cells = cells;
+  CK(occupancy_batch(B, static_cast<uint32_t *>(ctx->first_tri.p), ctx->build_tmp.p, ctx->build_tmp.cap, nullptr,
+                     ctx->num_sms, st));
   ENSURE(ctx->par_tmp, sparse_temp_bytes(cells, 0));
   uint64_t total = 0;
   CK(sparse_count(static_cast<const uint8_t *>(ctx->out_occ.p), cells, ctx->par_tmp.p, ctx->par_tmp.cap, &total, st));
@@ -566,13 +570,137 @@ sdfb_status sdfb_voxelize_sparse(sdfb_ctx *ctx, const float *positions, uint32_t
   std::vector<uint32_t> lin(n);
   if (n) CK(cudaMemcpyAsync(lin.data(), ctx->col_z.p, n * 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  const uint64_t r = uint64_t(resolution);
+  const uint64_t rr = uint64_t(resolution);
   for (uint64_t i = 0; i < n; ++i) {
     const uint64_t c = lin[i];
-    cells_out[3 * i] = static_cast<int32_t>(c % r);
-    cells_out[3 * i + 1] = static_cast<int32_t>((c / r) % r);
-    cells_out[3 * i + 2] = static_cast<int32_t>(c / (r * r));
+    cells_out[3 * i] = static_cast<int32_t>(c % rr);
+    cells_out[3 * i + 1] = static_cast<int32_t>((c / rr) % rr);
+    cells_out[3 * i + 2] = static_cast<int32_t>(c / (rr * rr));
   }
+  return SDFB_OK;
+}
+
+// ---- batched bake ------------------------------------------------------------------------------
+
+sdfb_status sdfb_bake_batch_device(sdfb_ctx *ctx, uint32_t count, const sdfb_mesh_desc *meshes,
+                                   const sdfb_grid_desc *grids, const sdfb_opts *opts, float *const *dist_outs,
+                                   uint8_t *const *occ_outs, void *stream, sdfb_stats *stats) {
+  if (!ctx) return SDFB_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if (count == 0 || !meshes || !grids) return ctx_fail(ctx, SDFB_ERR_INVALID_ARGUMENT, "empty batch");
+  cudaSetDevice(ctx->device);
+  const sdfb_opts o = opts_or_default(opts);
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  std::vector<PlanMesh> ms(count);
+  std::vector<CapBuild> caps(count);
+  bool any_gwn = false;
+  for (uint32_t m = 0; m < count; ++m) {
+    const sdfb_mesh_desc &d = meshes[m];
+    if (!d.verts || !d.idx || !grid_ok(&grids[m]))
+      return ctx_fail(ctx, SDFB_ERR_INVALID_ARGUMENT, "mesh %u: null pointer or invalid grid", m);
+    if (d.num_tris == 0 || d.num_verts == 0) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh %u has no triangles", m);
+    PlanMesh &p = ms[m];
+    p.verts = d.verts;
+    p.idx = d.idx;
+    p.V = d.num_verts;
+    p.T = d.num_tris;
+    p.grid = grids[m];
+    p.dist = (o.no_distance || !dist_outs) ? nullptr : dist_outs[m];
+    p.occ = (o.no_occupancy || !occ_outs) ? nullptr : occ_outs[m];
+    if (o.sign_mode == SDFB_SIGN_AUTO || o.sign_mode == SDFB_SIGN_GWN) {
+      std::vector<float> hv(size_t(d.num_verts) * 3);
+      std::vector<uint32_t> hi(size_t(d.num_tris) * 3);
+      CK(cudaMemcpyAsync(hv.data(), d.verts, hv.size() * 4, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(hi.data(), d.idx, hi.size() * 4, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      p.sign = resolve_sign(o, hv.data(), d.num_verts, hi.data(), d.num_tris, &p.watertight);
+      if (p.sign < 0) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh %u: triangle index out of range", m);
+      if (p.sign == kSignGwn && p.dist) {
+        for (size_t k = 0; k < hi.size(); ++k)
+          if (hi[k] >= d.num_verts) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh %u: triangle index out of range", m);
+        build_caps(hv.data(), d.num_verts, hi.data(), d.num_tris, caps[m]);
+        any_gwn = true;
+      }
+    } else {
+      p.sign = resolve_sign(o, nullptr, 0, nullptr, 0, &p.watertight);
+    }
+  }
+  if (any_gwn) {
+    const sdfb_status s = upload_caps(ctx, st, ms, caps);
+    if (s != SDFB_OK) return s;
+  }
+  return run_batch(ctx, st, ms, o, true, stats);
+}
+
+sdfb_status sdfb_bake_batch(sdfb_ctx *ctx, uint32_t count, const sdfb_mesh_desc *meshes, const sdfb_grid_desc *grids,
+                            const sdfb_opts *opts, float *const *dist_outs, uint8_t *const *occ_outs,
+                            sdfb_stats *stats) {
+  if (!ctx) return SDFB_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if (count == 0 || !meshes || !grids) return ctx_fail(ctx, SDFB_ERR_INVALID_ARGUMENT, "empty batch");
+  cudaSetDevice(ctx->device);
+  const sdfb_opts o = opts_or_default(opts);
+  const cudaStream_t st = ctx->stream;
+  size_t nv = 0, ni = 0;
+  uint64_t nc = 0;
+  for (uint32_t m = 0; m < count; ++m) {
+    if (!meshes[m].verts || !meshes[m].idx || !grid_ok(&grids[m]))
+      return ctx_fail(ctx, SDFB_ERR_INVALID_ARGUMENT, "mesh %u: null pointer or invalid grid", m);
+    if (meshes[m].num_tris == 0 || meshes[m].num_verts == 0)
+      return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh %u has no triangles", m);
+    nv += size_t(meshes[m].num_verts) * 3;
+    ni += size_t(meshes[m].num_tris) * 3;
+    nc += uint64_t(grids[m].nx) * grids[m].ny * grids[m].nz;
+  }
+  const bool want_dist = dist_outs && !o.no_distance, want_occ = occ_outs && !o.no_occupancy;
+  ENSURE(ctx->in_verts, nv * 4);
+  ENSURE(ctx->in_idx, ni * 4);
+  if (want_dist) ENSURE(ctx->out_dist, nc * 4);
+  if (want_occ) ENSURE(ctx->out_occ, nc);
+  std::vector<PlanMesh> ms(count);
+  std::vector<CapBuild> caps(count);
+  bool any_gwn = false;
+  size_t ov = 0, oi = 0;
+  uint64_t occ_off = 0;
+  for (uint32_t m = 0; m < count; ++m) {
+    const sdfb_mesh_desc &d = meshes[m];
+    PlanMesh &p = ms[m];
+    p.sign = resolve_sign(o, d.verts, d.num_verts, d.idx, d.num_tris, &p.watertight);
+    if (p.sign < 0) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh %u: triangle index out of range", m);
+    float *dv = static_cast<float *>(ctx->in_verts.p) + ov;
+    uint32_t *di = static_cast<uint32_t *>(ctx->in_idx.p) + oi;
+    CK(cudaMemcpyAsync(dv, d.verts, size_t(d.num_verts) * 12, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(di, d.idx, size_t(d.num_tris) * 12, cudaMemcpyHostToDevice, st));
+    p.verts = dv;
+    p.idx = di;
+    p.V = d.num_verts;
+    p.T = d.num_tris;
+    p.grid = grids[m];
+    const uint64_t cells = uint64_t(p.grid.nx) * p.grid.ny * p.grid.nz;
+    p.dist = (want_dist && dist_outs[m]) ? static_cast<float *>(ctx->out_dist.p) + occ_off : nullptr;
+    p.occ = (want_occ && occ_outs[m]) ? static_cast<uint8_t *>(ctx->out_occ.p) + occ_off : nullptr;
+    if (p.sign == kSignGwn && p.dist) {
+      for (size_t k = 0; k < size_t(d.num_tris) * 3; ++k)
+        if (d.idx[k] >= d.num_verts) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh %u: triangle index out of range", m);
+      build_caps(d.verts, d.num_verts, d.idx, d.num_tris, caps[m]);
+      any_gwn = true;
+    }
+    ov += size_t(d.num_verts) * 3;
+    oi += size_t(d.num_tris) * 3;
+    occ_off += cells;
+  }
+  if (any_gwn) {
+    const sdfb_status s = upload_caps(ctx, st, ms, caps);
+    if (s != SDFB_OK) return s;
+  }
+  const sdfb_status s = run_batch(ctx, st, ms, o, true, stats);
+  if (s != SDFB_OK) return s;
+  for (uint32_t m = 0; m < count; ++m) {
+    const uint64_t cells = uint64_t(ms[m].grid.nx) * ms[m].grid.ny * ms[m].grid.nz;
+    if (ms[m].dist) CK(cudaMemcpyAsync(dist_outs[m], ms[m].dist, cells * 4, cudaMemcpyDeviceToHost, st));
+    if (ms[m].occ) CK(cudaMemcpyAsync(occ_outs[m], ms[m].occ, cells, cudaMemcpyDeviceToHost, st));
+  }
+  CK(cudaStreamSynchronize(st));
   return SDFB_OK;
 }
 

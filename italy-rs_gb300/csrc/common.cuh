@@ -168,8 +168,10 @@ __device__ __forceinline__ int orient2_sos(float au, float av, float bu, float b
 }
 
 // Does the +z line through (px, py) cross triangle (a, b, c)? On a crossing *z receives the
-// crossing height (FP32 barycentric blend, within the triangle's z range).
-__device__ __forceinline__ bool column_crossing(f3 a, f3 b, f3 c, float px, float py, float &z) {
+// crossing height (FP32 barycentric blend, within the triangle's z range) and *s the crossing's
+// orientation: +1 when the triangle winds counter-clockwise seen from +z (its normal has a
+// positive z component, so the ray leaves an outward-oriented closed surface there), else -1.
+__device__ __forceinline__ bool column_crossing(f3 a, f3 b, f3 c, float px, float py, float &z, int &s) {
   float wab, wbc, wca;
   const int s0 = orient2_sos(a.x, a.y, b.x, b.y, px, py, wab);
   if (s0 == 0) return false;
@@ -185,6 +187,7 @@ __device__ __forceinline__ bool column_crossing(f3 a, f3 b, f3 c, float px, floa
   } else {
     z = (a.z + b.z + c.z) * (1.0f / 3.0f);
   }
+  s = s0;
   return true;
 }
 

@@ -23,7 +23,6 @@ namespace sdfb {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kStackDepth = 64;
 
 struct Shape {
   int tx, ty, tz;
@@ -31,29 +30,35 @@ struct Shape {
 constexpr Shape kShapes[] = {{4, 4, 2}, {8, 4, 1}, {4, 4, 4}, {8, 4, 2}, {4, 4, 8}, {8, 4, 4}};
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
-template <int TX, int TY, int TZ, bool COUNT>
-__global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a, long long num_tiles, int tiles_x,
-                                                       int tiles_y) {
+template <int TX, int TY, int TZ, int STACK, bool COUNT>
+__global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a) {
   constexpr int kLayer = TX * TY;
   constexpr int kLanesZ = kWarp / kLayer;
   constexpr int VPL = TZ / kLanesZ;
   static_assert(kLayer * kLanesZ == kWarp && VPL * kLanesZ == TZ, "tile must cover whole warps");
+  static_assert(STACK == 32 || STACK == 64, "stack depth is one or two registers per lane");
   const int lane = threadIdx.x & 31;
   const int lx = lane % TX, ly = (lane / TX) % TY, lz = lane / kLayer;
-  const GridDev g = a.g;
+  const BatchDev &B = a.batch;
   unsigned long long box_tests = 0, tri_tests = 0;
   bool overflow = false, corrupt = false;
   // A correct tree expands each inner node at most once per tile and pops at most once per
   // push; anything longer means a corrupt tree, and the walk stops with an error.
   const long long step_limit = 2ll * a.num_nodes + 64;
+  const int num_tris = static_cast<int>(B.total_tris);
 
   for (;;) {
-    long long tile = 0;
-    if (lane == 0) tile = static_cast<long long>(atomicAdd(a.tile_counter, 1ull));
+    unsigned long long tile = 0;
+    if (lane == 0) tile = atomicAdd(a.tile_counter, 1ull);
     tile = __shfl_sync(kFull, tile, 0);
-    if (tile >= num_tiles) break;
-    const int tx = static_cast<int>(tile % tiles_x);
-    const long long rest = tile / tiles_x;
+    if (tile >= B.total_tiles) break;
+    const int mesh = find_mesh(B.tile_starts, B.num_meshes, tile);
+    const MeshRec &M = B.recs[mesh];
+    const GridDev g = M.g;
+    const unsigned long long local = tile - B.tile_starts[mesh];
+    const int tiles_x = (g.nx + TX - 1) / TX, tiles_y = (g.ny + TY - 1) / TY;
+    const int tx = static_cast<int>(local % tiles_x);
+    const unsigned long long rest = local / tiles_x;
     const int ty = static_cast<int>(rest % tiles_y);
     const int tz = static_cast<int>(rest / tiles_y);
     const int vx = tx * TX + lx, vy = ty * TY + ly;
@@ -69,7 +74,7 @@ __global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a, long long
     }
 
     auto test_leaf = [&](int first, int count) {
-      if (first < 0 || count > a.num_tris - first) {
+      if (first < 0 || count > num_tris - first) {
         corrupt = true;
         return;
       }
@@ -82,16 +87,16 @@ __global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a, long long
       if (COUNT) tri_tests += static_cast<unsigned long long>(count) * kWarp * VPL;
     };
 
-    int cur = 0, sp = 0, stk0 = 0, stk1 = 0;
+    int cur = M.root, sp = 0, stk0 = 0, stk1 = 0;
     for (long long steps = 0;; ++steps) {
-      if (steps > step_limit || (cur >= a.num_nodes)) {
+      if (steps > step_limit || cur >= a.num_nodes) {
         corrupt = true;
         break;
       }
       if (cur < 0) {
         if (sp == 0) break;
         --sp;
-        const int e = __shfl_sync(kFull, sp < 32 ? stk0 : stk1, sp & 31);
+        const int e = __shfl_sync(kFull, (STACK == 32 || sp < 32) ? stk0 : stk1, sp & 31);
         if ((e >> 1) >= a.num_nodes) {
           corrupt = true;
           break;
@@ -159,9 +164,9 @@ __global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a, long long
       }
       if (far_w) {
         if (cur >= 0) {
-          if (sp < kStackDepth) {
+          if (sp < STACK) {
             const int e = (node << 1) | (second_first ? 0 : 1);
-            if (sp < 32) {
+            if (STACK == 32 || sp < 32) {
               if (lane == sp) stk0 = e;
             } else if (lane == sp - 32) {
               stk1 = e;
@@ -182,8 +187,8 @@ __global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a, long long
     int inside[VPL];
 #pragma unroll
     for (int v = 0; v < VPL; ++v) inside[v] = 0;
-    if (a.sign == kSignParity && vx < g.nx && vy < g.ny) {
-      const uint64_t col = uint64_t(vy) * g.nx + vx;
+    if (M.sign == kSignParity && vx < g.nx && vy < g.ny) {
+      const uint64_t col = M.col_base + uint64_t(vy) * g.nx + vx;
       const uint64_t s0 = __ldg(a.col_start + col), s1 = __ldg(a.col_start + col + 1);
       for (uint64_t k = s0; k < s1; ++k) {
         const float zc = __ldg(a.col_z + k);
@@ -197,7 +202,7 @@ __global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a, long long
       const int vz = tz * TZ + lz + v * kLanesZ;
       const uint64_t cell = (uint64_t(vz) * g.ny + vy) * g.nx + vx;
       const float d = sqrtf(best[v]);
-      a.dist[cell] = inside[v] ? -d : d;
+      M.dist[cell] = inside[v] ? -d : d;
     }
   }
   if (overflow) atomic_or_err(a.err, kErrStackOverflow);
@@ -208,38 +213,34 @@ __global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a, long long
   }
 }
 
-template <int I, bool COUNT>
+template <int I, int STACK, bool COUNT>
 cudaError_t launch_shape(const DistanceArgs &a, int num_sms, cudaStream_t st) {
   constexpr Shape s = kShapes[I];
-  const int tiles_x = (a.g.nx + s.tx - 1) / s.tx, tiles_y = (a.g.ny + s.ty - 1) / s.ty,
-            tiles_z = (a.g.nz + s.tz - 1) / s.tz;
-  const long long num_tiles = static_cast<long long>(tiles_x) * tiles_y * tiles_z;
   static int per_sm = 0;
   if (per_sm == 0) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_distance<s.tx, s.ty, s.tz, COUNT>, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_distance<s.tx, s.ty, s.tz, STACK, COUNT>, kThreads, 0);
     if (per_sm <= 0) per_sm = 1;
   }
-  const long long warps_needed = num_tiles;
-  long long blocks = static_cast<long long>(num_sms) * per_sm;
-  blocks = std::min<long long>(blocks, (warps_needed + (kThreads / kWarp) - 1) / (kThreads / kWarp));
+  const unsigned long long warps_needed = a.batch.total_tiles;
+  unsigned long long blocks = static_cast<unsigned long long>(num_sms) * per_sm;
+  blocks = std::min<unsigned long long>(blocks, (warps_needed + (kThreads / kWarp) - 1) / (kThreads / kWarp));
   if (blocks < 1) blocks = 1;
   cudaError_t e = cudaMemsetAsync(a.tile_counter, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
-  k_distance<s.tx, s.ty, s.tz, COUNT><<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(a, num_tiles, tiles_x,
-                                                                                          tiles_y);
+  k_distance<s.tx, s.ty, s.tz, STACK, COUNT><<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(a);
   note_launch();
   return cudaGetLastError();
 }
 
-template <bool COUNT>
+template <int STACK, bool COUNT>
 cudaError_t launch_any(const DistanceArgs &a, int id, int num_sms, cudaStream_t st) {
   switch (id) {
-    case 0: return launch_shape<0, COUNT>(a, num_sms, st);
-    case 1: return launch_shape<1, COUNT>(a, num_sms, st);
-    case 2: return launch_shape<2, COUNT>(a, num_sms, st);
-    case 3: return launch_shape<3, COUNT>(a, num_sms, st);
-    case 4: return launch_shape<4, COUNT>(a, num_sms, st);
-    default: return launch_shape<5, COUNT>(a, num_sms, st);
+    case 0: return launch_shape<0, STACK, COUNT>(a, num_sms, st);
+    case 1: return launch_shape<1, STACK, COUNT>(a, num_sms, st);
+    case 2: return launch_shape<2, STACK, COUNT>(a, num_sms, st);
+    case 3: return launch_shape<3, STACK, COUNT>(a, num_sms, st);
+    case 4: return launch_shape<4, STACK, COUNT>(a, num_sms, st);
+    default: return launch_shape<5, STACK, COUNT>(a, num_sms, st);
   }
 }
 
@@ -254,9 +255,20 @@ void tile_shape(int id, int &tx, int &ty, int &tz) {
   tz = s.tz;
 }
 
-cudaError_t distance_launch(const DistanceArgs &a, int tile_id, int num_sms, cudaStream_t st) {
-  if (a.work_counters) return launch_any<true>(a, tile_id, num_sms, st);
-  return launch_any<false>(a, tile_id, num_sms, st);
+uint64_t tiles_for(const GridDev &g, int id) {
+  int tx, ty, tz;
+  tile_shape(id, tx, ty, tz);
+  return uint64_t((g.nx + tx - 1) / tx) * uint64_t((g.ny + ty - 1) / ty) * uint64_t((g.nz + tz - 1) / tz);
+}
+
+cudaError_t distance_launch(const DistanceArgs &a, int tile_id, int stack_depth, int num_sms, cudaStream_t st) {
+  if (a.batch.total_tiles == 0) return cudaSuccess;
+  if (stack_depth <= 32) {
+    if (a.work_counters) return launch_any<32, true>(a, tile_id, num_sms, st);
+    return launch_any<32, false>(a, tile_id, num_sms, st);
+  }
+  if (a.work_counters) return launch_any<64, true>(a, tile_id, num_sms, st);
+  return launch_any<64, false>(a, tile_id, num_sms, st);
 }
 
 }  // namespace sdfb

@@ -1,20 +1,23 @@
 // Generalized winding number sign for meshes that are not watertight (replaces the 5-ray parity
 // vote of src/render/kernels/sdf_bake.cu:53-69, which assumes a closed mesh).
 //
-// w(q) = sum over triangles of the signed solid angle / 4 pi (Jacobson, Kavan & Sorkine-Hornung
-// 2013); a cell is inside when |w| > 0.5. Solid angles are exact for near triangles
-// (Van Oosterom & Strackee 1983) and far clusters use the dipole expansion of Barill et al. 2018
-// kept to the second term: w_node = (N . r / d^3 + tr(M) / d^3 - 3 r^T M r / d^5) / (4 pi) with
-// r = P - q, using the moments stored per inner node by lbvh.cu. A cluster counts as far when
-// every cell of the warp's tile is more than beta * radius from P.
+// w(q) = sum of triangle solid angles / 4 pi (Jacobson, Kavan & Sorkine-Hornung 2013); a cell is
+// inside when |w| > 0.5. It is evaluated through an exact decomposition: the host closes every
+// boundary loop of the mesh with a small fan cap (host_mesh.cpp), so mesh + caps has no boundary
+// and its winding number W(q) is an integer, namely the signed count of +z crossings above q
+// (parity.cu stores each crossing's orientation). Then
+//     w(q) = W(q) - w_caps(q),
+// and only the caps -- small triangles hugging the holes -- need solid angles. A cap subtree
+// whose box is at distance d from q subtends at most (area / d^2), so far caps are bounded rather
+// than summed, and a cell is decided as soon as the bound cannot move |w| across 0.5.
 //
 // Precision split:
-//   pass 1 (FP32, every cell, warp tiles, beta = 2): cells farther than band_voxels from the
-//     surface whose |w| is clear of 0.5 by more than the accumulated truncation estimate get their
-//     sign; all others (the band and ambiguous cells) are appended to a refine list.
-//   pass 2 (FP64 accumulation and arithmetic, beta = 3, exact triangles from the original FP32
-//     vertices): signs of the refine list; a cell still within its FP64 estimate of 0.5 goes to
-//   pass 3 (FP64 direct sum over every triangle, one block per cell).
+//   pass 1 (FP32, every cell of every winding-number mesh, warp tiles of 4 x 4 x 2): cells
+//     outside the band (|d| > band_voxels * voxel) whose interval [c - e, c + e] lies on one side
+//     of |w| = 0.5 get their sign; the band and undecided cells go to a refine list.
+//   pass 2 (FP64 accumulation and arithmetic, exact caps from the original FP32 vertices, far
+//     bound threshold 1e-9 sr): signs of the refine list; a cell still undecided goes to
+//   pass 3 (FP64 sum over every cap triangle of its mesh, one block per cell).
 #include <algorithm>
 #include <cstdint>
 
@@ -27,15 +30,15 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kStack = 64;
-constexpr float kBeta32 = 2.0f;
-constexpr double kBeta64 = 3.0;
 constexpr double kInv4Pi = 0.07957747154594767;
+constexpr float kTau32 = 4e-3f;   // sr: expand cap subtrees that may subtend more
+constexpr double kTau64 = 1e-9;
 
 template <typename T> struct V3 {
   T x, y, z;
 };
 
-// Exact solid angle of triangle (a, b, c) seen from q (Van Oosterom & Strackee).
+// Exact solid angle of triangle (a, b, c) seen from the origin (Van Oosterom & Strackee 1983).
 template <typename T>
 __device__ __forceinline__ T solid_angle(V3<T> a, V3<T> b, V3<T> c) {
   const T la = sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
@@ -48,253 +51,259 @@ __device__ __forceinline__ T solid_angle(V3<T> a, V3<T> b, V3<T> c) {
   return T(2) * atan2(det, den);
 }
 
-// Second-order dipole expansion of one node at q; adds the truncation estimate A r^2 3/(4pi (d-r)^4).
-template <typename T>
-__device__ __forceinline__ T expand(const float4 &m0, const float4 &m1, const float4 &m2, const float4 &m3, T qx, T qy,
-                                    T qz, T &err) {
-  const T rx = T(m0.x) - qx, ry = T(m0.y) - qy, rz = T(m0.z) - qz;
-  const T d2 = rx * rx + ry * ry + rz * rz;
-  const T d = sqrt(d2);
-  const T inv_d3 = T(1) / (d2 * d);
-  const T M[9] = {T(m1.w), T(m2.x), T(m2.y), T(m2.z), T(m2.w), T(m3.x), T(m3.y), T(m3.z), T(m3.w)};
-  const T nr = T(m1.x) * rx + T(m1.y) * ry + T(m1.z) * rz;
-  const T tr = M[0] + M[4] + M[8];
-  const T Mr0 = M[0] * rx + M[1] * ry + M[2] * rz, Mr1 = M[3] * rx + M[4] * ry + M[5] * rz,
-          Mr2 = M[6] * rx + M[7] * ry + M[8] * rz;
-  const T rMr = rx * Mr0 + ry * Mr1 + rz * Mr2;
-  const T rad = T(m0.w);
-  const T area = sqrt(T(m1.x) * T(m1.x) + T(m1.y) * T(m1.y) + T(m1.z) * T(m1.z));
-  const T gap = d - rad;
-  err += T(3) * area * rad * rad / (gap * gap * gap * gap);
-  return (nr + tr) * inv_d3 - T(3) * rMr * inv_d3 / d2;
-}
-
 struct GwnArgs {
-  const Node *nodes;
-  const TriRec *tris;
-  const float4 *mom;
-  const uint32_t *leaf_order;
-  const float *verts;
-  const uint32_t *idx;
-  int num_nodes, num_tris;
-  GridDev g;
-  float band;            // distance below which a cell is in the band
-  float *dist;           // unsigned on entry, signed on exit
-  uint32_t *refine;      // list of cells for the FP64 pass
+  BatchDev batch;
+  const uint64_t *col_start;
+  const float *col_z;
+  const int8_t *col_s;
+  const Node *cap_nodes;
+  const TriRec *cap_tris;
+  const float *cap_area;       // per inner node of the caps hierarchy
+  const uint32_t *cap_order;   // local cap triangle of each cap record
+  int cap_num_nodes, cap_num_inner, cap_num_tris;
+  float band_voxels;
+  float *dummy;
+  uint64_t *refine;
   unsigned long long *refine_count;
+  uint64_t *direct;
+  unsigned long long *direct_count;
   unsigned long long *tile_counter;
   uint32_t *err;
 };
 
-// Pass 1: FP32 over warp tiles of 4 x 4 x 2 cells.
-__global__ __launch_bounds__(kThreads) void k_gwn32(GwnArgs a, long long num_tiles, int tiles_x, int tiles_y) {
+// Signed crossings of the column above height pz (the integer winding number of mesh + caps).
+__device__ __forceinline__ int column_winding(const GwnArgs &a, const MeshRec &M, int vx, int vy, float pz) {
+  const uint64_t col = M.col_base + uint64_t(vy) * M.g.nx + vx;
+  const uint64_t s0 = __ldg(a.col_start + col), s1 = __ldg(a.col_start + col + 1);
+  int w = 0;
+  for (uint64_t k = s0; k < s1; ++k)
+    if (__ldg(a.col_z + k) > pz) w += __ldg(a.col_s + k);
+  return w;
+}
+
+__device__ __forceinline__ float box_d2(float px, float py, float pz, const float4 &n0, const float4 &n1,
+                                        const float4 &n2, int which) {
+  if (which == 0) return box_dist2(px, py, pz, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
+  return box_dist2(px, py, pz, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
+}
+
+// Caps of one mesh seen from q, warp-uniform walk: exact solid angles where some lane needs them,
+// bounds (area / d^2) elsewhere. T is the arithmetic type; exact FP64 leaves read the original
+// cap vertices.
+template <typename T, bool EXACT64>
+__device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, T qx, T qy, T qz, float tau, T &wex,
+                          T &eps, bool &corrupt) {
+  const int lane = threadIdx.x & 31;
+  int cur = M.cap_root, sp = 0, stk0 = 0, stk1 = 0;
+  const long long step_limit = 2ll * a.cap_num_nodes + 64;
+  const float fx = float(qx), fy = float(qy), fz = float(qz);
+  auto push = [&](int e) {
+    if (sp < kStack) {
+      if (sp < 32) {
+        if (lane == sp) stk0 = e;
+      } else if (lane == sp - 32) {
+        stk1 = e;
+      }
+      ++sp;
+    } else {
+      corrupt = true;
+    }
+  };
+  for (long long steps = 0;; ++steps) {
+    if (cur < 0) {
+      if (sp == 0) break;
+      --sp;
+      cur = __shfl_sync(kFull, sp < 32 ? stk0 : stk1, sp & 31);
+    }
+    if (steps > step_limit || cur >= a.cap_num_nodes) {
+      corrupt = true;
+      break;
+    }
+    const Node *np = a.cap_nodes + cur;
+    const float4 n0 = __ldg(&np->n0), n1 = __ldg(&np->n1), n2 = __ldg(&np->n2);
+    const int4 n3 = __ldg(&np->n3);
+    const int refs[2] = {n3.x, n3.y}, cnts[2] = {n3.z, n3.w};
+    int next = -1;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      if (cnts[k] < 0) continue;
+      const float d2 = box_d2(fx, fy, fz, n0, n1, n2, k);
+      float area;
+      if (cnts[k] == 0) {
+        if (refs[k] >= a.cap_num_inner) {
+          corrupt = true;
+          continue;
+        }
+        area = __ldg(a.cap_area + refs[k]);
+      } else {
+        if (refs[k] < 0 || cnts[k] > a.cap_num_tris - refs[k]) {
+          corrupt = true;
+          continue;
+        }
+        area = 0.0f;
+        for (int j = 0; j < cnts[k]; ++j) {
+          const float4 r3 = __ldg(&a.cap_tris[refs[k] + j].r3);
+          area += 0.5f * sqrtf(r3.x * r3.x + r3.y * r3.y + r3.z * r3.z);
+        }
+      }
+      const float bound = d2 > 0.0f ? area / d2 : __int_as_float(0x7f800000);
+      const bool need = active && !(bound <= tau);
+      if (!__any_sync(kFull, need)) {
+        if (active) eps += T(bound);
+        continue;
+      }
+      if (cnts[k] == 0) {
+        if (next < 0) next = refs[k];
+        else push(refs[k]);
+        continue;
+      }
+      for (int j = 0; j < cnts[k]; ++j) {
+        if (EXACT64) {
+          const uint32_t t = __ldg(a.cap_order + refs[k] + j);
+          V3<T> p[3];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const uint32_t i = __ldg(M.cidx + 3ull * t + c);
+            p[c] = {T(__ldg(M.cverts + 3ull * i)) - qx, T(__ldg(M.cverts + 3ull * i + 1)) - qy,
+                    T(__ldg(M.cverts + 3ull * i + 2)) - qz};
+          }
+          wex += solid_angle<T>(p[0], p[1], p[2]);
+        } else {
+          const TriRec *tr = a.cap_tris + refs[k] + j;
+          const float4 r0 = __ldg(&tr->r0), r1 = __ldg(&tr->r1), r2 = __ldg(&tr->r2);
+          const V3<T> p{T(r0.x) - qx, T(r0.y) - qy, T(r0.z) - qz};
+          wex += solid_angle<T>(p, {p.x + T(r1.x), p.y + T(r1.y), p.z + T(r1.z)},
+                                {p.x + T(r2.x), p.y + T(r2.y), p.z + T(r2.z)});
+        }
+      }
+    }
+    cur = next;
+  }
+}
+
+// Pass 1: FP32 over warp tiles of 4 x 4 x 2 cells of the winding-number meshes.
+__global__ __launch_bounds__(kThreads) void k_gwn32(GwnArgs a) {
   constexpr int TX = 4, TY = 4, TZ = 2;
   const int lane = threadIdx.x & 31;
   const int lx = lane % TX, ly = (lane / TX) % TY, lz = lane / (TX * TY);
-  const GridDev g = a.g;
+  const BatchDev &B = a.batch;
   bool corrupt = false;
-  const long long step_limit = 2ll * a.num_nodes + 64;
   for (;;) {
-    long long tile = 0;
-    if (lane == 0) tile = static_cast<long long>(atomicAdd(a.tile_counter, 1ull));
+    unsigned long long tile = 0;
+    if (lane == 0) tile = atomicAdd(a.tile_counter, 1ull);
     tile = __shfl_sync(kFull, tile, 0);
-    if (tile >= num_tiles) break;
-    const int tx = static_cast<int>(tile % tiles_x);
-    const long long rest = tile / tiles_x;
+    if (tile >= B.total_gwn_tiles) break;
+    const int mesh = find_mesh(B.gwn_tile_starts, B.num_meshes, tile);
+    const MeshRec &M = B.recs[mesh];
+    const GridDev g = M.g;
+    const unsigned long long local = tile - B.gwn_tile_starts[mesh];
+    const int tiles_x = (g.nx + TX - 1) / TX, tiles_y = (g.ny + TY - 1) / TY;
+    const int tx = static_cast<int>(local % tiles_x);
+    const unsigned long long rest = local / tiles_x;
     const int ty = static_cast<int>(rest % tiles_y), tz = static_cast<int>(rest / tiles_y);
     const int vx = tx * TX + lx, vy = ty * TY + ly, vz = tz * TZ + lz;
     const bool active = vx < g.nx && vy < g.ny && vz < g.nz;
     const float qx = cell_center(g.ox, vx, g.voxel), qy = cell_center(g.oy, vy, g.voxel),
                 qz = cell_center(g.oz, vz, g.voxel);
-    float w = 0.0f, err = 0.0f;
-    int cur = 0, sp = 0, stk0 = 0, stk1 = 0;
-    auto leaf = [&](int first, int count) {
-      if (first < 0 || count > a.num_tris - first) {
-        corrupt = true;
-        return;
-      }
-      for (int k = 0; k < count; ++k) {
-        const TriRec *tr = a.tris + first + k;
-        const float4 r0 = __ldg(&tr->r0), r1 = __ldg(&tr->r1), r2 = __ldg(&tr->r2);
-        const V3<float> p{r0.x - qx, r0.y - qy, r0.z - qz};
-        w += solid_angle<float>(p, {p.x + r1.x, p.y + r1.y, p.z + r1.z}, {p.x + r2.x, p.y + r2.y, p.z + r2.z});
-      }
-    };
-    auto push = [&](int e) {
-      if (sp < kStack) {
-        if (sp < 32) {
-          if (lane == sp) stk0 = e;
-        } else if (lane == sp - 32) {
-          stk1 = e;
-        }
-        ++sp;
-      } else {
-        corrupt = true;
-      }
-    };
-    for (long long steps = 0;; ++steps) {
-      if (cur < 0) {
-        if (sp == 0) break;
-        --sp;
-        cur = __shfl_sync(kFull, sp < 32 ? stk0 : stk1, sp & 31);
-      }
-      if (steps > step_limit || cur >= a.num_nodes) {
-        corrupt = true;
-        break;
-      }
-      const int4 n3 = __ldg(&a.nodes[cur].n3);
-      const int refs[2] = {n3.x, n3.y}, cnts[2] = {n3.z, n3.w};
-      int next = -1;
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        if (cnts[k] < 0) continue;
-        if (cnts[k] > 0) {
-          leaf(refs[k], cnts[k]);
-          continue;
-        }
-        const float4 *mp = a.mom + 4ll * refs[k];
-        const float4 m0 = __ldg(mp), m1 = __ldg(mp + 1);
-        const float dx = m0.x - qx, dy = m0.y - qy, dz = m0.z - qz;
-        const bool far = dx * dx + dy * dy + dz * dz > (kBeta32 * m0.w) * (kBeta32 * m0.w);
-        if (__all_sync(kFull, far || !active)) {
-          w += expand<float>(m0, m1, __ldg(mp + 2), __ldg(mp + 3), qx, qy, qz, err);
-        } else if (next < 0) {
-          next = refs[k];
-        } else {
-          push(refs[k]);
-        }
-      }
-      cur = next;
-    }
+    float wex = 0.0f, eps = 0.0f;
+    if (M.cap_root >= 0) caps_walk<float, false>(a, M, active, qx, qy, qz, kTau32, wex, eps, corrupt);
     if (!active) continue;
+    const int W = column_winding(a, M, vx, vy, qz);
     const uint64_t cell = (uint64_t(vz) * g.ny + vy) * g.nx + vx;
-    const float d = a.dist[cell];
-    const float aw = fabsf(w * static_cast<float>(kInv4Pi));
-    const float e = err * static_cast<float>(kInv4Pi) + 1e-4f + 1e-5f * fabsf(w);
-    if (d <= a.band || fabsf(aw - 0.5f) <= e) {
+    const float d = M.dist[cell];
+    const float c = fabsf(float(W) - wex * float(kInv4Pi));
+    const float e = eps * float(kInv4Pi) + 1e-5f * (1.0f + fabsf(wex));
+    const bool band = d <= a.band_voxels * g.voxel;
+    if (!band && c - e > 0.5f) {
+      M.dist[cell] = -d;
+    } else if (band || !(c + e < 0.5f)) {
       const unsigned long long at = atomicAdd(a.refine_count, 1ull);
-      a.refine[at] = static_cast<uint32_t>(cell);
-    } else if (aw > 0.5f) {
-      a.dist[cell] = -d;
+      a.refine[at] = B.cell_starts[mesh] + cell;
     }
   }
   if (corrupt) atomic_or_err(a.err, kErrCorruptTree);
 }
 
-// Pass 2: FP64, one cell per lane (cells from the refine list), exact triangles from the original
-// vertices. Cells still ambiguous are appended to the direct-sum list.
-__global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a, unsigned long long n, uint32_t *direct,
-                                                    unsigned long long *direct_count) {
+__device__ __forceinline__ void cell_of(const BatchDev &B, uint64_t gcell, int &mesh, int &vx, int &vy, int &vz,
+                                        uint64_t &cell) {
+  mesh = find_mesh(B.cell_starts, B.num_meshes, gcell);
+  const GridDev &g = B.recs[mesh].g;
+  cell = gcell - B.cell_starts[mesh];
+  vx = static_cast<int>(cell % uint64_t(g.nx));
+  vy = static_cast<int>((cell / uint64_t(g.nx)) % uint64_t(g.ny));
+  vz = static_cast<int>(cell / (uint64_t(g.nx) * g.ny));
+}
+
+// Pass 2: FP64, one refine cell per lane.
+__global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a, unsigned long long n) {
   const int lane = threadIdx.x & 31;
-  const GridDev g = a.g;
+  const BatchDev &B = a.batch;
   bool corrupt = false;
-  const long long step_limit = 2ll * a.num_nodes + 64;
   const unsigned long long warps = (unsigned long long)gridDim.x * (kThreads / kWarp);
   for (unsigned long long base = (blockIdx.x * (kThreads / kWarp) + (threadIdx.x >> 5)) * 32ull; base < n;
        base += warps * 32ull) {
     const unsigned long long k = base + lane;
     const bool active = k < n;
-    const uint32_t cell = active ? a.refine[k] : 0u;
-    const int vx = static_cast<int>(cell % uint32_t(g.nx)), vy = static_cast<int>((cell / uint32_t(g.nx)) % uint32_t(g.ny)),
-              vz = static_cast<int>(cell / (uint32_t(g.nx) * uint32_t(g.ny)));
-    const double qx = cell_center(g.ox, vx, g.voxel), qy = cell_center(g.oy, vy, g.voxel),
-                 qz = cell_center(g.oz, vz, g.voxel);
-    double w = 0.0, err = 0.0;
-    int cur = 0, sp = 0, stk0 = 0, stk1 = 0;
-    auto vert = [&](uint32_t i) -> V3<double> {
-      return {double(__ldg(a.verts + 3ull * i)) - qx, double(__ldg(a.verts + 3ull * i + 1)) - qy,
-              double(__ldg(a.verts + 3ull * i + 2)) - qz};
-    };
-    auto leaf = [&](int first, int count) {
-      if (first < 0 || count > a.num_tris - first) {
-        corrupt = true;
-        return;
+    int mesh, vx, vy, vz;
+    uint64_t cell;
+    cell_of(B, active ? a.refine[k] : a.refine[base], mesh, vx, vy, vz, cell);
+    const MeshRec &M = B.recs[mesh];
+    const GridDev g = M.g;
+    const float fz = cell_center(g.oz, vz, g.voxel);
+    const double qx = cell_center(g.ox, vx, g.voxel), qy = cell_center(g.oy, vy, g.voxel), qz = fz;
+    double wex = 0.0, eps = 0.0;
+    // lanes of one warp may belong to different meshes: walk each distinct mesh in turn
+    const int first_mesh = __shfl_sync(kFull, mesh, 0);
+    const bool uniform = __all_sync(kFull, mesh == first_mesh);
+    if (uniform) {
+      if (M.cap_root >= 0) caps_walk<double, true>(a, M, active, qx, qy, qz, float(kTau64), wex, eps, corrupt);
+    } else {
+      unsigned pending = __ballot_sync(kFull, true);
+      while (pending) {
+        const int leader = __ffs(pending) - 1;
+        const int mm = __shfl_sync(kFull, mesh, leader);
+        const bool mine = mesh == mm;
+        const MeshRec &MM = B.recs[mm];
+        if (MM.cap_root >= 0)
+          caps_walk<double, true>(a, MM, active && mine, qx, qy, qz, float(kTau64), wex, eps, corrupt);
+        pending &= ~__ballot_sync(kFull, mine);
       }
-      for (int j = 0; j < count; ++j) {
-        const uint32_t t = __ldg(a.leaf_order + first + j);
-        w += solid_angle<double>(vert(__ldg(a.idx + 3ull * t)), vert(__ldg(a.idx + 3ull * t + 1)),
-                                 vert(__ldg(a.idx + 3ull * t + 2)));
-      }
-    };
-    auto push = [&](int e) {
-      if (sp < kStack) {
-        if (sp < 32) {
-          if (lane == sp) stk0 = e;
-        } else if (lane == sp - 32) {
-          stk1 = e;
-        }
-        ++sp;
-      } else {
-        corrupt = true;
-      }
-    };
-    for (long long steps = 0;; ++steps) {
-      if (cur < 0) {
-        if (sp == 0) break;
-        --sp;
-        cur = __shfl_sync(kFull, sp < 32 ? stk0 : stk1, sp & 31);
-      }
-      if (steps > step_limit || cur >= a.num_nodes) {
-        corrupt = true;
-        break;
-      }
-      const int4 n3 = __ldg(&a.nodes[cur].n3);
-      const int refs[2] = {n3.x, n3.y}, cnts[2] = {n3.z, n3.w};
-      int next = -1;
-#pragma unroll
-      for (int c = 0; c < 2; ++c) {
-        if (cnts[c] < 0) continue;
-        if (cnts[c] > 0) {
-          leaf(refs[c], cnts[c]);
-          continue;
-        }
-        const float4 *mp = a.mom + 4ll * refs[c];
-        const float4 m0 = __ldg(mp), m1 = __ldg(mp + 1);
-        const double dx = double(m0.x) - qx, dy = double(m0.y) - qy, dz = double(m0.z) - qz;
-        const double lim = kBeta64 * double(m0.w);
-        const bool far = dx * dx + dy * dy + dz * dz > lim * lim;
-        if (__all_sync(kFull, far || !active)) {
-          w += expand<double>(m0, m1, __ldg(mp + 2), __ldg(mp + 3), qx, qy, qz, err);
-        } else if (next < 0) {
-          next = refs[c];
-        } else {
-          push(refs[c]);
-        }
-      }
-      cur = next;
     }
     if (!active) continue;
-    const double aw = fabs(w * kInv4Pi);
-    const double e = err * kInv4Pi + 1e-9;
-    if (fabs(aw - 0.5) <= e) {
-      const unsigned long long at = atomicAdd(direct_count, 1ull);
-      direct[at] = cell;
-    } else if (aw > 0.5) {
-      a.dist[cell] = -fabsf(a.dist[cell]);
+    const int W = column_winding(a, M, vx, vy, fz);
+    const double c = fabs(double(W) - wex * kInv4Pi);
+    const double e = eps * kInv4Pi + 1e-12 * (1.0 + fabs(wex));
+    if (c - e > 0.5) {
+      M.dist[cell] = -fabsf(M.dist[cell]);
+    } else if (!(c + e < 0.5)) {
+      const unsigned long long at = atomicAdd(a.direct_count, 1ull);
+      a.direct[at] = a.refine[k];
     }
   }
   if (corrupt) atomic_or_err(a.err, kErrCorruptTree);
 }
 
-// Pass 3: one block per remaining cell, FP64 direct sum over every triangle.
-__global__ __launch_bounds__(kThreads) void k_gwn_direct(GwnArgs a, const uint32_t *cells,
-                                                         const unsigned long long *count) {
+// Pass 3: one block per remaining cell, FP64 sum over every cap triangle of its mesh.
+__global__ __launch_bounds__(kThreads) void k_gwn_direct(GwnArgs a) {
   __shared__ double part[kThreads / kWarp];
-  const GridDev g = a.g;
-  for (unsigned long long k = blockIdx.x; k < *count; k += gridDim.x) {
-    const uint32_t cell = cells[k];
-    const int vx = static_cast<int>(cell % uint32_t(g.nx)), vy = static_cast<int>((cell / uint32_t(g.nx)) % uint32_t(g.ny)),
-              vz = static_cast<int>(cell / (uint32_t(g.nx) * uint32_t(g.ny)));
-    const double qx = cell_center(g.ox, vx, g.voxel), qy = cell_center(g.oy, vy, g.voxel),
-                 qz = cell_center(g.oz, vz, g.voxel);
+  const BatchDev &B = a.batch;
+  const unsigned long long n = *a.direct_count;
+  for (unsigned long long k = blockIdx.x; k < n; k += gridDim.x) {
+    int mesh, vx, vy, vz;
+    uint64_t cell;
+    cell_of(B, a.direct[k], mesh, vx, vy, vz, cell);
+    const MeshRec &M = B.recs[mesh];
+    const GridDev g = M.g;
+    const float fz = cell_center(g.oz, vz, g.voxel);
+    const double qx = cell_center(g.ox, vx, g.voxel), qy = cell_center(g.oy, vy, g.voxel), qz = fz;
     double w = 0.0;
-    for (int t = threadIdx.x; t < a.num_tris; t += kThreads) {
+    for (uint32_t t = threadIdx.x; t < M.cap_tris; t += kThreads) {
       V3<double> p[3];
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        const uint32_t i = __ldg(a.idx + 3ull * t + j);
-        p[j] = {double(__ldg(a.verts + 3ull * i)) - qx, double(__ldg(a.verts + 3ull * i + 1)) - qy,
-                double(__ldg(a.verts + 3ull * i + 2)) - qz};
+        const uint32_t i = __ldg(M.cidx + 3ull * t + j);
+        p[j] = {double(__ldg(M.cverts + 3ull * i)) - qx, double(__ldg(M.cverts + 3ull * i + 1)) - qy,
+                double(__ldg(M.cverts + 3ull * i + 2)) - qz};
       }
       w += solid_angle<double>(p[0], p[1], p[2]);
     }
@@ -305,7 +314,8 @@ __global__ __launch_bounds__(kThreads) void k_gwn_direct(GwnArgs a, const uint32
     if (threadIdx.x == 0) {
       double s = 0.0;
       for (int i = 0; i < kThreads / kWarp; ++i) s += part[i];
-      if (fabs(s * kInv4Pi) > 0.5) a.dist[cell] = -fabsf(a.dist[cell]);
+      const int W = column_winding(a, M, vx, vy, fz);
+      if (fabs(double(W) - s * kInv4Pi) > 0.5) M.dist[cell] = -fabsf(M.dist[cell]);
     }
     __syncthreads();
   }
@@ -313,57 +323,54 @@ __global__ __launch_bounds__(kThreads) void k_gwn_direct(GwnArgs a, const uint32
 
 }  // namespace
 
-sdfb_status gwn_apply(sdfb_ctx *ctx, cudaStream_t st, const MeshDev &m, const BakeInput &in,
-                      const sdfb_grid_desc &grid, const sdfb_opts &opts, float *d_dist, uint32_t *d_err) {
-  if (!m.moments) return ctx_fail(ctx, SDFB_ERR_INTERNAL, "winding-number moments were not built");
-  const uint64_t cells = uint64_t(grid.nx) * grid.ny * grid.nz;
-  if (cells >= (1ull << 32))
-    return ctx_fail(ctx, SDFB_ERR_INVALID_ARGUMENT, "winding-number sign supports grids below 2^32 cells");
-  // refine list + direct list + counters
-  const size_t need = cells * 4 + 256 + cells * 4 + 256;
-  if (!ctx->gwn_tmp.ensure(need)) return ctx_fail(ctx, SDFB_ERR_OUT_OF_MEMORY, "winding-number workspace");
+sdfb_status gwn_apply(sdfb_ctx *ctx, cudaStream_t st, const GwnInput &in) {
+  const BatchDev &B = in.batch;
+  if (B.total_gwn_tiles == 0) return SDFB_OK;
+  const uint64_t cells = in.gwn_cells;
+  const size_t list_bytes = ((cells * 8 + 255) & ~size_t(255));
+  if (!ctx->gwn_tmp.ensure(256 + 2 * list_bytes))
+    return ctx_fail(ctx, SDFB_ERR_OUT_OF_MEMORY, "winding-number workspace");
   char *base = static_cast<char *>(ctx->gwn_tmp.p);
   unsigned long long *counters = reinterpret_cast<unsigned long long *>(base);  // [0] tiles [1] refine [2] direct
-  uint32_t *refine = reinterpret_cast<uint32_t *>(base + 256);
-  uint32_t *direct = reinterpret_cast<uint32_t *>(base + 256 + ((cells * 4 + 255) & ~255ull));
+  GwnArgs a;
+  a.batch = B;
+  a.col_start = in.col_start;
+  a.col_z = in.col_z;
+  a.col_s = in.col_s;
+  a.cap_nodes = in.caps.nodes;
+  a.cap_tris = in.caps.tris;
+  a.cap_area = in.caps.node_area;
+  a.cap_order = in.caps.leaf_order;
+  a.cap_num_nodes = in.caps.num_nodes;
+  a.cap_num_inner = in.caps.num_inner;
+  a.cap_num_tris = static_cast<int>(in.cap_total_tris);
+  a.band_voxels = in.band_voxels;
+  a.refine = reinterpret_cast<uint64_t *>(base + 256);
+  a.refine_count = counters + 1;
+  a.direct = reinterpret_cast<uint64_t *>(base + 256 + list_bytes);
+  a.direct_count = counters + 2;
+  a.tile_counter = counters;
+  a.err = in.err;
   cudaError_t e = cudaMemsetAsync(counters, 0, 64, st);
   if (e != cudaSuccess) return ctx_cuda(ctx, e, "memset");
-  GwnArgs a;
-  a.nodes = m.nodes;
-  a.tris = m.tris;
-  a.mom = m.moments;
-  a.leaf_order = m.leaf_order;
-  a.verts = in.verts;
-  a.idx = in.idx;
-  a.num_nodes = static_cast<int>(std::max<uint32_t>(m.num_tris, 2) - 1);
-  a.num_tris = static_cast<int>(m.num_tris);
-  a.g = to_dev(grid);
-  a.band = opts.band_voxels * grid.voxel_size;
-  a.dist = d_dist;
-  a.refine = refine;
-  a.refine_count = counters + 1;
-  a.tile_counter = counters;
-  a.err = d_err;
-  const int tiles_x = (grid.nx + 3) / 4, tiles_y = (grid.ny + 3) / 4, tiles_z = (grid.nz + 1) / 2;
-  const long long num_tiles = static_cast<long long>(tiles_x) * tiles_y * tiles_z;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gwn32, kThreads, 0);
   long long blocks = static_cast<long long>(ctx->num_sms) * std::max(per_sm, 1);
-  blocks = std::min<long long>(blocks, (num_tiles + 7) / 8);
-  k_gwn32<<<static_cast<unsigned>(std::max<long long>(blocks, 1)), kThreads, 0, st>>>(a, num_tiles, tiles_x, tiles_y);
+  blocks = std::min<long long>(blocks, static_cast<long long>((B.total_gwn_tiles + 7) / 8));
+  k_gwn32<<<static_cast<unsigned>(std::max<long long>(blocks, 1)), kThreads, 0, st>>>(a);
   note_launch();
   if ((e = cudaGetLastError()) != cudaSuccess) return ctx_cuda(ctx, e, "k_gwn32");
-  // The refine count sizes pass 2's grid: read it back (the bake synchronises at its end anyway).
+  // The refine count sizes pass 2: read it back (the bake synchronises at its end anyway).
   unsigned long long n_refine = 0;
   if ((e = cudaMemcpyAsync(&n_refine, counters + 1, 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
       (e = cudaStreamSynchronize(st)) != cudaSuccess)
     return ctx_cuda(ctx, e, "refine count");
   if (n_refine) {
     const unsigned long long warps = (n_refine + 31) / 32;
-    const unsigned g2 = static_cast<unsigned>(std::min<unsigned long long>((warps + 7) / 8, 65535ull * 8));
-    k_gwn64<<<std::max(g2, 1u), kThreads, 0, st>>>(a, n_refine, direct, counters + 2);
+    const unsigned g2 = static_cast<unsigned>(std::min<unsigned long long>((warps + 7) / 8, 1ull << 20));
+    k_gwn64<<<std::max(g2, 1u), kThreads, 0, st>>>(a, n_refine);
     note_launch();
-    k_gwn_direct<<<static_cast<unsigned>(ctx->num_sms * 4), kThreads, 0, st>>>(a, direct, counters + 2);
+    k_gwn_direct<<<static_cast<unsigned>(ctx->num_sms * 4), kThreads, 0, st>>>(a);
     note_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return ctx_cuda(ctx, e, "k_gwn64");
   }

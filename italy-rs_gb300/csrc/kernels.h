@@ -1,5 +1,9 @@
 // Host-side launch interface of the bake kernels. Every launcher enqueues work on the given
 // stream and returns the launch error (cudaSuccess when it was enqueued).
+//
+// All stages work on a batch of meshes at once: triangles, cells, columns and tiles of the meshes
+// are numbered consecutively ("global" indices), each kernel finds the mesh of a global index by
+// binary search over a prefix table, and a single mesh is simply a batch of one.
 #pragma once
 
 #include <cstddef>
@@ -11,20 +15,20 @@ namespace sdfb {
 struct TriRec;
 struct Node;
 
-// Device scratch for the device-wide primitives; grown by the caller (see Workspace in api.cu).
-struct Scratch {
-  void *ptr = nullptr;
-  size_t bytes = 0;
-};
-
 // Count of kernel launches issued by this library (every launcher calls note_launch once per
 // <<<...>>>); the bake reports the launches of one call in sdfb_stats.
 void note_launch();
 uint64_t launch_count();
 
+// Device scratch for the device-wide primitives.
+struct Scratch {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+};
+
 // ---- primitives.cu ----------------------------------------------------------------------------
-// Exclusive scan of n uint32 counts into uint64 starts; starts[n] receives the total, so `out`
-// must hold n + 1 values. Scratch need: scan_scratch_bytes(n).
+// Exclusive scan of n uint32 counts into uint64 starts; out[n] receives the total, so `out` must
+// hold n + 1 values. Scratch need: scan_scratch_bytes(n).
 size_t scan_scratch_bytes(size_t n);
 cudaError_t exclusive_scan_u32(const uint32_t *in, uint64_t *out, size_t n, Scratch s, cudaStream_t st);
 
@@ -34,77 +38,114 @@ size_t sort_scratch_bytes(size_t n);
 cudaError_t radix_sort_pairs(uint64_t *keys, uint32_t *vals, uint64_t *keys_alt, uint32_t *vals_alt, size_t n,
                              int bits, Scratch s, cudaStream_t st);
 
-// ---- lbvh.cu ----------------------------------------------------------------------------------
-// One mesh's device-resident acceleration structure.
-struct MeshDev {
-  uint32_t num_verts = 0, num_tris = 0;
-  const float *verts = nullptr;     // V x 3 (original positions; occupancy and parity read these)
-  const uint32_t *idx = nullptr;    // T x 3
-  TriRec *tris = nullptr;           // T records in leaf order
-  Node *nodes = nullptr;            // max(T - 1, 1) nodes, root = 0
-  uint32_t *leaf_order = nullptr;   // original triangle index of each record
-  uint32_t *bounds = nullptr;       // 6 ordered-uint words: min xyz, max xyz
-  float4 *moments = nullptr;        // optional: 4 float4 per inner node (winding-number expansion)
-  int leaf_size = 1;
-};
-
-// Temporaries of one build, sized by lbvh_temp_bytes(T).
-size_t lbvh_temp_bytes(uint32_t num_tris);
-// tris + nodes + leaf_order + bounds (+ moments when with_moments)
-size_t lbvh_mesh_bytes(uint32_t num_tris, bool with_moments = false);
-// Carves a MeshDev's arrays out of `mem` (lbvh_mesh_bytes(T, with_moments) bytes, 256-aligned).
-void lbvh_bind_mesh(MeshDev &m, void *mem, bool with_moments = false);
-// Builds the hierarchy; when m.moments is set it also fills the winding-number moments.
-cudaError_t lbvh_build(MeshDev &m, int leaf_size, void *temp, size_t temp_bytes, uint32_t *err, cudaStream_t st);
-
-// ---- occupancy.cu -----------------------------------------------------------------------------
+// ---- the batch ---------------------------------------------------------------------------------
 struct GridDev {
   float ox, oy, oz, voxel;
   int nx, ny, nz;
 };
 
-size_t occupancy_temp_bytes(uint32_t num_tris);
-// occ must hold nx * ny * nz bytes; it is cleared and then filled. sat_tests (optional device
-// uint64) receives the number of SAT tests.
-cudaError_t occupancy_dense(const float *verts, const uint32_t *idx, uint32_t num_verts, uint32_t num_tris, GridDev g,
-                            uint8_t *occ, void *temp, size_t temp_bytes, unsigned long long *sat_tests,
-                            cudaStream_t st);
-// Variant that also records, per occupied cell, the smallest triangle index that hits it
-// (first_tri must hold nx*ny*nz uint32 and is initialised here).
-cudaError_t occupancy_dense_first(const float *verts, const uint32_t *idx, uint32_t num_verts, uint32_t num_tris,
-                                  GridDev g, uint8_t *occ, uint32_t *first_tri, void *temp, size_t temp_bytes,
-                                  cudaStream_t st);
+enum SignKind : int { kSignNone = 0, kSignParity = 1, kSignGwn = 2 };
+
+// Device-side record of one mesh of a batch.
+struct MeshRec {
+  const float *verts;     // V x 3, original positions (occupancy, parity and FP64 winding read these)
+  const uint32_t *idx;    // T x 3, local vertex indices
+  const float *pverts;    // the mesh whose crossings decide parity (== verts unless a welded copy)
+  const uint32_t *pidx;
+  float *dist;            // cell outputs (either may be null)
+  uint8_t *occ;
+  uint32_t num_verts, num_tris, pnum_verts, pnum_tris;
+  uint64_t tri_base;      // first global triangle = first sorted position of this mesh
+  uint64_t cell_base;     // first global cell
+  uint64_t col_base;      // first global column (parity meshes only)
+  GridDev g;
+  int sign;               // SignKind
+  int leaf_size;          // 1..16
+  int root;               // virtual root node of this mesh (see lbvh.cu)
+  int cap_root;           // GWN: virtual root of this mesh's caps in the caps hierarchy, -1 if none
+  const float *cverts;    // GWN: vertices of the caps (the parity mesh's vertices + loop centres)
+  const uint32_t *cidx;   // GWN: cap triangles
+  uint32_t cap_tris;      // GWN: number of cap triangles
+  uint32_t pad;
+};
+
+// Prefix tables of a batch (device): starts[m] of each numbering, starts[M] = total.
+struct BatchDev {
+  int num_meshes = 0;
+  const MeshRec *recs = nullptr;
+  const uint64_t *tri_starts = nullptr;       // triangles (BVH, occupancy)
+  const uint64_t *ptri_starts = nullptr;      // triangles of the parity meshes
+  const uint64_t *tile_starts = nullptr;      // distance tiles
+  const uint64_t *gwn_tile_starts = nullptr;  // winding-number tiles (only GWN meshes have any)
+  const uint64_t *cell_starts = nullptr;      // cells
+  uint64_t total_tris = 0, total_ptris = 0, total_cells = 0, total_cols = 0, total_tiles = 0, total_gwn_tiles = 0;
+};
+
+// Largest m in [0, n) with starts[m] <= x (starts[0] = 0).
+__host__ __device__ __forceinline__ int find_mesh(const uint64_t *starts, int n, uint64_t x) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (starts[mid] <= x) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// ---- lbvh.cu ----------------------------------------------------------------------------------
+// The batch's acceleration structure: every mesh's triangles, sorted by (mesh, Morton code), under
+// one binary radix tree; each mesh's subtree is entered through its virtual root node, stored
+// after the inner nodes.
+struct BvhDev {
+  TriRec *tris = nullptr;          // T_total records in leaf order
+  Node *nodes = nullptr;           // (T_total - 1) inner nodes + M virtual roots
+  uint32_t *leaf_order = nullptr;  // local (per-mesh) triangle index of each record
+  uint32_t *bounds = nullptr;      // 6 ordered-uint words per mesh: centroid min xyz, max xyz
+  float *node_area = nullptr;      // optional: total triangle area per inner node
+  int num_inner = 0;               // max(T_total - 1, 0)
+  int num_nodes = 0;               // num_inner + M
+};
+
+size_t lbvh_temp_bytes(uint64_t total_tris, int num_meshes);
+size_t lbvh_bytes(uint64_t total_tris, int num_meshes, bool with_areas);
+void lbvh_bind(BvhDev &b, void *mem, uint64_t total_tris, int num_meshes, bool with_areas);
+cudaError_t lbvh_build(const BatchDev &batch, BvhDev &b, void *temp, size_t temp_bytes, uint32_t *err,
+                       cudaStream_t st);
+
+// ---- occupancy.cu -----------------------------------------------------------------------------
+size_t occupancy_temp_bytes(uint64_t total_tris);
+// Clears and fills every mesh's occ grid (meshes with occ == null are skipped). first_tri
+// (optional, for a batch of one) receives per cell the smallest triangle index that hits it.
+cudaError_t occupancy_batch(const BatchDev &batch, uint32_t *first_tri, void *temp, size_t temp_bytes,
+                            unsigned long long *sat_tests, int num_sms, cudaStream_t st);
 
 // ---- parity.cu --------------------------------------------------------------------------------
-// Column crossing lists for +z parity: col_start[nx*ny + 1] (uint64 starts), col_z[capacity].
-size_t parity_temp_bytes(uint32_t num_tris, int nx, int ny);
-cudaError_t parity_columns(const float *verts, const uint32_t *idx, uint32_t num_verts, uint32_t num_tris, GridDev g,
-                           uint64_t *col_start,
-                           float *col_z, uint64_t capacity, void *temp, size_t temp_bytes, uint32_t *err,
+// Column crossing lists along +z over the parity and winding-number meshes (their pverts / pidx):
+// col_start[total_cols + 1] (uint64 starts), col_z[capacity] heights, col_s[capacity] orientations.
+size_t parity_temp_bytes(uint64_t total_ptris, uint64_t total_cols);
+cudaError_t parity_columns(const BatchDev &batch, uint64_t *col_start, float *col_z, int8_t *col_s,
+                           uint64_t capacity, void *temp, size_t temp_bytes, uint32_t *err, int num_sms,
                            cudaStream_t st);
 
 // ---- distance.cu ------------------------------------------------------------------------------
-enum SignKind : int { kSignNone = 0, kSignParity = 1, kSignGwn = 2 };
-
 struct DistanceArgs {
+  BatchDev batch;
   const Node *nodes;
   const TriRec *tris;
-  int num_nodes;  // inner nodes (max(T - 1, 1))
-  int num_tris;
-  GridDev g;
-  int sign;
+  int num_nodes;              // inner nodes + virtual roots
   const uint64_t *col_start;  // parity
   const float *col_z;
-  float *dist;
   uint32_t *err;
-  unsigned long long *tile_counter;      // zeroed by the launcher
-  unsigned long long *work_counters;     // optional: [0] box tests, [1] triangle tests (lanes)
+  unsigned long long *tile_counter;   // zeroed by the launcher
+  unsigned long long *work_counters;  // optional: [0] box tests, [1] triangle tests (lanes)
 };
 
 int tile_shape_count();
 // tile shape id -> (tx, ty, tz)
 void tile_shape(int id, int &tx, int &ty, int &tz);
-cudaError_t distance_launch(const DistanceArgs &a, int tile_id, int num_sms, cudaStream_t st);
+uint64_t tiles_for(const GridDev &g, int tile_id);
+// stack_depth: 32 or 64 entries (32 keeps the stack in one register per lane).
+cudaError_t distance_launch(const DistanceArgs &a, int tile_id, int stack_depth, int num_sms, cudaStream_t st);
 
 // ---- sparse.cu --------------------------------------------------------------------------------
 size_t sparse_temp_bytes(size_t cells, size_t max_out);

@@ -1,17 +1,21 @@
-// Device-built linear BVH over one mesh's triangles (replaces the OptiX GAS build of
-// src/convert/sdf_baker.cpp:170-193).
+// Device-built linear BVH over the triangles of a batch of meshes (replaces the OptiX GAS build
+// of src/convert/sdf_baker.cpp:170-193, which builds one acceleration structure per call).
 //
-//   1. k_prep      gathers each indexed triangle, checks indices and finiteness, writes its
-//                  64-byte distance record and bounds, and reduces the centroid bounds.
-//   2. k_morton    30-bit Morton code of the box centre, normalised to the centroid bounds.
-//   3. radix sort  (code, triangle) pairs, stable.
-//   4. k_hierarchy binary radix tree over the sorted codes (Karras 2012, "Maximizing Parallelism
-//                  in the Construction of BVHs, Octrees, and k-d Trees"; equal codes ordered by
-//                  position), one thread per inner node.
+//   1. k_prep      gathers each indexed triangle of each mesh, checks indices and finiteness,
+//                  writes its 64-byte distance record and box, and reduces per-mesh centroid bounds.
+//   2. k_morton    key = (mesh << 30) | 30-bit Morton code of the box centre in its mesh's bounds.
+//   3. radix sort  (key, triangle) pairs, stable: meshes end up contiguous, each in Morton order.
+//   4. k_hierarchy binary radix tree over all keys (Karras 2012, "Maximizing Parallelism in the
+//                  Construction of BVHs, Octrees, and k-d Trees"; equal keys ordered by position).
+//                  Since keys of one mesh share the mesh prefix, each mesh owns one subtree.
 //   5. k_refit     bottom-up boxes: the second thread to reach a node merges its children.
-//   6. k_layout    64-byte traversal nodes holding both child boxes; subtrees of at most
-//                  `leaf_size` triangles become leaves (their records are contiguous).
-//   7. k_gather    triangle records in leaf order.
+//   6. k_layout    64-byte traversal nodes holding both child boxes; subtrees of at most the
+//                  mesh's leaf size become leaves (their records are contiguous).
+//   7. k_roots     one virtual root node per mesh, after the inner nodes, whose first child is
+//                  the mesh's subtree (or leaf) and whose second child is empty; traversal of a
+//                  mesh starts there.
+//   8. k_gather    triangle records in leaf order.
+//   9. k_areas     (optional) total triangle area per inner node.
 #include <algorithm>
 #include <cstdint>
 
@@ -26,8 +30,8 @@ constexpr int kThreads = 256;
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 struct BuildTemp {
-  TriRec *rec;      // T, original order
-  float4 *lo, *hi;  // T, triangle boxes (original order)
+  TriRec *rec;      // T, global triangle order
+  float4 *lo, *hi;  // T, triangle boxes (global triangle order)
   uint64_t *keys, *keys_alt;
   uint32_t *vals, *vals_alt;
   int2 *child;      // T - 1: (left, right); leaf children have the top bit set
@@ -36,12 +40,13 @@ struct BuildTemp {
   int *lparent;     // T
   int *visits;      // T - 1
   float4 *ilo, *ihi;  // T - 1 inner boxes
+  int *subtree;     // M: inner node covering exactly the mesh, -1 if none
   void *scratch;
   size_t scratch_bytes;
 };
 
-size_t temp_layout(uint32_t T, char *base, BuildTemp *t) {
-  const size_t n = std::max<uint32_t>(T, 1), m = std::max<uint32_t>(T, 2) - 1;
+size_t temp_layout(uint64_t T, int M, char *base, BuildTemp *t) {
+  const size_t n = std::max<uint64_t>(T, 1), m = std::max<uint64_t>(T, 2) - 1;
   size_t off = 0;
   auto take = [&](size_t bytes) {
     char *p = base ? base + off : nullptr;
@@ -63,6 +68,7 @@ size_t temp_layout(uint32_t T, char *base, BuildTemp *t) {
   x.visits = reinterpret_cast<int *>(take(m * 4));
   x.ilo = reinterpret_cast<float4 *>(take(m * sizeof(float4)));
   x.ihi = reinterpret_cast<float4 *>(take(m * sizeof(float4)));
+  x.subtree = reinterpret_cast<int *>(take(size_t(M) * 4));
   x.scratch_bytes = sort_scratch_bytes(n);
   x.scratch = take(x.scratch_bytes);
   if (t) *t = x;
@@ -82,21 +88,25 @@ __device__ __forceinline__ float3 load3(const float *v, uint32_t i) {
   return make_float3(__ldg(v + 3ull * i), __ldg(v + 3ull * i + 1), __ldg(v + 3ull * i + 2));
 }
 
-__global__ __launch_bounds__(kThreads) void k_prep(const float *__restrict__ verts, const uint32_t *__restrict__ idx,
-                                                   uint32_t V, uint32_t T, TriRec *__restrict__ rec,
-                                                   float4 *__restrict__ lo, float4 *__restrict__ hi,
-                                                   uint32_t *__restrict__ bounds, uint32_t *__restrict__ err) {
-  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+__global__ __launch_bounds__(kThreads) void k_prep(BatchDev B, TriRec *__restrict__ rec, float4 *__restrict__ lo,
+                                                   float4 *__restrict__ hi, uint32_t *__restrict__ bounds,
+                                                   uint32_t *__restrict__ err) {
+  const uint64_t t = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
   float cmin[3] = {INFINITY, INFINITY, INFINITY}, cmax[3] = {-INFINITY, -INFINITY, -INFINITY};
-  if (t < T) {
-    uint32_t i0 = __ldg(idx + 3ull * t), i1 = __ldg(idx + 3ull * t + 1), i2 = __ldg(idx + 3ull * t + 2);
+  int mesh = -1;
+  if (t < B.total_tris) {
+    mesh = find_mesh(B.tri_starts, B.num_meshes, t);
+    const MeshRec &M = B.recs[mesh];
+    const uint64_t lt = t - B.tri_starts[mesh];
+    const uint32_t V = M.num_verts;
+    uint32_t i0 = __ldg(M.idx + 3 * lt), i1 = __ldg(M.idx + 3 * lt + 1), i2 = __ldg(M.idx + 3 * lt + 2);
     if (i0 >= V || i1 >= V || i2 >= V) {
       atomic_or_err(err, kErrBadIndex);
       i0 = i0 < V ? i0 : 0;
       i1 = i1 < V ? i1 : 0;
       i2 = i2 < V ? i2 : 0;
     }
-    const float3 a = load3(verts, i0), b = load3(verts, i1), c = load3(verts, i2);
+    const float3 a = load3(M.verts, i0), b = load3(M.verts, i1), c = load3(M.verts, i2);
     const bool finite = isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(b.x) && isfinite(b.y) &&
                         isfinite(b.z) && isfinite(c.x) && isfinite(c.y) && isfinite(c.z);
     if (!finite) atomic_or_err(err, kErrNonFinite);
@@ -120,45 +130,49 @@ __global__ __launch_bounds__(kThreads) void k_prep(const float *__restrict__ ver
     lo[t] = l;
     hi[t] = h;
     if (finite) {
-      const float cx = 0.5f * (l.x + h.x), cy = 0.5f * (l.y + h.y), cz = 0.5f * (l.z + h.z);
-      cmin[0] = cmax[0] = cx;
-      cmin[1] = cmax[1] = cy;
-      cmin[2] = cmax[2] = cz;
+      cmin[0] = cmax[0] = 0.5f * (l.x + h.x);
+      cmin[1] = cmax[1] = 0.5f * (l.y + h.y);
+      cmin[2] = cmax[2] = 0.5f * (l.z + h.z);
     }
   }
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      cmin[a] = fminf(cmin[a], __shfl_xor_sync(kFull, cmin[a], o));
-      cmax[a] = fmaxf(cmax[a], __shfl_xor_sync(kFull, cmax[a], o));
-    }
-  }
-  if ((threadIdx.x & 31) == 0 && cmin[0] <= cmax[0]) {
+  // Reduce over the warp when all its lanes hold the same mesh, else per lane.
+  const int m0 = __shfl_sync(kFull, mesh, 0);
+  if (__all_sync(kFull, mesh == m0)) {
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      atomicMin(bounds + a, float_to_ordered(cmin[a]));
-      atomicMax(bounds + 3 + a, float_to_ordered(cmax[a]));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        cmin[a] = fminf(cmin[a], __shfl_xor_sync(kFull, cmin[a], o));
+        cmax[a] = fmaxf(cmax[a], __shfl_xor_sync(kFull, cmax[a], o));
+      }
+    }
+    if ((threadIdx.x & 31) != 0) mesh = -1;
+  }
+  if (mesh >= 0 && cmin[0] <= cmax[0]) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      atomicMin(bounds + 6 * mesh + a, float_to_ordered(cmin[a]));
+      atomicMax(bounds + 6 * mesh + 3 + a, float_to_ordered(cmax[a]));
     }
   }
 }
 
-__global__ void k_init_bounds(uint32_t *bounds) {
-  if (threadIdx.x < 3) bounds[threadIdx.x] = 0xffffffffu;       // min
-  else if (threadIdx.x < 6) bounds[threadIdx.x] = 0u;           // max
+__global__ void k_init_bounds(uint32_t *bounds, int M) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < 6 * M) bounds[i] = (i % 6) < 3 ? 0xffffffffu : 0u;
 }
 
-__global__ __launch_bounds__(kThreads) void k_morton(const float4 *__restrict__ lo, const float4 *__restrict__ hi,
-                                                     uint32_t T, const uint32_t *__restrict__ bounds,
+__global__ __launch_bounds__(kThreads) void k_morton(BatchDev B, const float4 *__restrict__ lo,
+                                                     const float4 *__restrict__ hi, const uint32_t *__restrict__ bounds,
                                                      uint64_t *__restrict__ keys, uint32_t *__restrict__ vals) {
-  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
-  if (t >= T) return;
+  const uint64_t t = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
+  if (t >= B.total_tris) return;
+  const int mesh = find_mesh(B.tri_starts, B.num_meshes, t);
   float bmin[3], ext[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    bmin[a] = ordered_to_float(bounds[a]);
-    const float bmax = ordered_to_float(bounds[3 + a]);
-    ext[a] = bmax - bmin[a];
+    bmin[a] = ordered_to_float(bounds[6 * mesh + a]);
+    ext[a] = ordered_to_float(bounds[6 * mesh + 3 + a]) - bmin[a];
   }
   const float4 l = lo[t], h = hi[t];
   const float c[3] = {0.5f * (l.x + h.x), 0.5f * (l.y + h.y), 0.5f * (l.z + h.z)};
@@ -169,8 +183,8 @@ __global__ __launch_bounds__(kThreads) void k_morton(const float4 *__restrict__ 
     const float s = fminf(fmaxf(u * 1024.0f, 0.0f), 1023.0f);
     q[a] = isfinite(s) ? static_cast<uint32_t>(s) : 0u;
   }
-  keys[t] = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
-  vals[t] = t;
+  keys[t] = (uint64_t(mesh) << 30) | (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+  vals[t] = static_cast<uint32_t>(t);
 }
 
 // Length of the common prefix of sorted keys i and j (positions break ties); -1 outside.
@@ -218,6 +232,16 @@ __global__ __launch_bounds__(kThreads) void k_hierarchy(const uint64_t *__restri
   child[i] = make_int2(left, right);
   range[i] = make_int2(first, last);
   if (i == 0) iparent[0] = -1;
+}
+
+// The inner node whose range is exactly one mesh's triangles is that mesh's subtree root.
+__global__ __launch_bounds__(kThreads) void k_find_subtrees(BatchDev B, const uint64_t *__restrict__ keys, int n,
+                                                            const int2 *__restrict__ range, int *__restrict__ subtree) {
+  const int i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= n - 1) return;
+  const int2 r = range[i];
+  const int mesh = static_cast<int>(keys[r.x] >> 30);
+  if (uint64_t(r.x) == B.tri_starts[mesh] && uint64_t(r.y) + 1 == B.tri_starts[mesh + 1]) subtree[mesh] = i;
 }
 
 __device__ __forceinline__ void child_box(int c, const uint32_t *__restrict__ vals, const float4 *__restrict__ lo,
@@ -273,21 +297,16 @@ __device__ __forceinline__ void store_node(Node *nodes, int i, const float *b, i
   nodes[i] = nd;
 }
 
-__global__ __launch_bounds__(kThreads) void k_layout(int n, int leaf_size, const uint32_t *__restrict__ vals,
-                                                     const float4 *__restrict__ lo, const float4 *__restrict__ hi,
-                                                     const int2 *__restrict__ child, const int2 *__restrict__ range,
-                                                     const float4 *__restrict__ ilo, const float4 *__restrict__ ihi,
-                                                     Node *__restrict__ nodes) {
+__global__ __launch_bounds__(kThreads) void k_layout(BatchDev B, int n, const uint64_t *__restrict__ keys,
+                                                     const uint32_t *__restrict__ vals, const float4 *__restrict__ lo,
+                                                     const float4 *__restrict__ hi, const int2 *__restrict__ child,
+                                                     const int2 *__restrict__ range, const float4 *__restrict__ ilo,
+                                                     const float4 *__restrict__ ihi, Node *__restrict__ nodes) {
   const int i = blockIdx.x * kThreads + threadIdx.x;
   if (i >= n - 1) return;
+  const int leaf_size = B.recs[keys[range[i].x] >> 30].leaf_size;
   float box[12];
   int ref[2], cnt[2];
-  if (i == 0 && n <= leaf_size) {  // the whole mesh is one leaf
-    put_child(box, 0, ilo[0], ihi[0]);
-    put_child(box, 1, make_float4(INFINITY, INFINITY, INFINITY, 0), make_float4(-INFINITY, -INFINITY, -INFINITY, 0));
-    store_node(nodes, 0, box, make_int4(0, 0, n, -1));
-    return;
-  }
   const int2 c = child[i];
   const int cs[2] = {c.x, c.y};
 #pragma unroll
@@ -318,100 +337,59 @@ __global__ __launch_bounds__(kThreads) void k_layout(int n, int leaf_size, const
   store_node(nodes, i, box, make_int4(ref[0], ref[1], cnt[0], cnt[1]));
 }
 
-__global__ void k_single(const float4 *lo, const float4 *hi, Node *nodes) {
+// Virtual root of each mesh: child 0 is the mesh's subtree (a leaf range when the mesh has at
+// most leaf_size triangles), child 1 is empty.
+__global__ void k_roots(BatchDev B, int num_inner, const uint32_t *__restrict__ vals, const float4 *__restrict__ lo,
+                        const float4 *__restrict__ hi, const float4 *__restrict__ ilo,
+                        const float4 *__restrict__ ihi, const int *__restrict__ subtree, Node *__restrict__ nodes,
+                        uint32_t *__restrict__ err) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= B.num_meshes) return;
+  const MeshRec &M = B.recs[m];
+  const int first = static_cast<int>(B.tri_starts[m]);
+  const int count = static_cast<int>(B.tri_starts[m + 1] - B.tri_starts[m]);
   float box[12];
-  put_child(box, 0, lo[0], hi[0]);
-  put_child(box, 1, make_float4(INFINITY, INFINITY, INFINITY, 0), make_float4(-INFINITY, -INFINITY, -INFINITY, 0));
-  store_node(nodes, 0, box, make_int4(0, 0, 1, -1));
+  const float4 empty_lo = make_float4(INFINITY, INFINITY, INFINITY, 0), empty_hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0);
+  put_child(box, 1, empty_lo, empty_hi);
+  int4 refs = make_int4(0, 0, -1, -1);
+  if (count == 1) {
+    const uint32_t t = vals[first];
+    put_child(box, 0, lo[t], hi[t]);
+    refs = make_int4(first, 0, 1, -1);
+  } else if (count > 1) {
+    const int s = subtree[m];
+    if (s < 0) {
+      atomic_or_err(err, kErrCorruptTree);
+      put_child(box, 0, empty_lo, empty_hi);
+    } else {
+      put_child(box, 0, ilo[s], ihi[s]);
+      refs = count <= M.leaf_size ? make_int4(first, 0, count, -1) : make_int4(s, 0, 0, -1);
+    }
+  } else {
+    put_child(box, 0, empty_lo, empty_hi);
+  }
+  store_node(nodes, num_inner + m, box, refs);
 }
 
-__global__ __launch_bounds__(kThreads) void k_gather(uint32_t T, const uint32_t *__restrict__ vals,
+__global__ __launch_bounds__(kThreads) void k_gather(BatchDev B, const uint32_t *__restrict__ vals,
                                                      const TriRec *__restrict__ rec, TriRec *__restrict__ out,
                                                      uint32_t *__restrict__ order) {
-  const uint32_t k = blockIdx.x * kThreads + threadIdx.x;
-  if (k >= T) return;
-  const uint32_t t = vals ? vals[k] : k;
+  const uint64_t k = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
+  if (k >= B.total_tris) return;
+  const uint32_t t = vals ? vals[k] : static_cast<uint32_t>(k);
   out[k] = rec[t];
-  order[k] = t;
+  order[k] = static_cast<uint32_t>(t - B.tri_starts[find_mesh(B.tri_starts, B.num_meshes, t)]);
 }
 
-// Winding-number moments of every inner node, bottom-up like k_refit (Barill et al. 2018, "Fast
-// Winding Numbers for Soups and Clouds": each triangle is a dipole of area vector a = (e1 x e2)/2
-// at its centroid c; a node keeps N = sum a, P = area-weighted centroid, M = sum a (c - P)^T and
-// r = radius around P). Children combine as N = N0 + N1, P = (A0 P0 + A1 P1) / (A0 + A1),
-// M = M0 + N0 (P0 - P)^T + M1 + N1 (P1 - P)^T, r = max(r0 + |P0 - P|, r1 + |P1 - P|).
-struct Mom {
-  float px, py, pz, r, nx, ny, nz, area;
-  float m[9];
-};
-
-__device__ __forceinline__ Mom leaf_mom(const TriRec &t) {
-  Mom o;
-  const float cx = t.r0.x + (t.r1.x + t.r2.x) * (1.0f / 3.0f);
-  const float cy = t.r0.y + (t.r1.y + t.r2.y) * (1.0f / 3.0f);
-  const float cz = t.r0.z + (t.r1.z + t.r2.z) * (1.0f / 3.0f);
-  o.px = cx;
-  o.py = cy;
-  o.pz = cz;
-  o.nx = 0.5f * t.r3.x;
-  o.ny = 0.5f * t.r3.y;
-  o.nz = 0.5f * t.r3.z;
-  o.area = sqrtf(o.nx * o.nx + o.ny * o.ny + o.nz * o.nz);
-  const float ax = t.r0.x - cx, ay = t.r0.y - cy, az = t.r0.z - cz;
-  const float bx = ax + t.r1.x, by = ay + t.r1.y, bz = az + t.r1.z;
-  const float qx = ax + t.r2.x, qy = ay + t.r2.y, qz = az + t.r2.z;
-  o.r = sqrtf(fmaxf(fmaxf(ax * ax + ay * ay + az * az, bx * bx + by * by + bz * bz), qx * qx + qy * qy + qz * qz));
-#pragma unroll
-  for (int k = 0; k < 9; ++k) o.m[k] = 0.0f;
-  return o;
+// Total triangle area of every inner node, bottom-up like k_refit (bounds the solid angle a
+// subtree can subtend: at distance d from its box it is at most area / d^2).
+__device__ __forceinline__ float tri_area(const TriRec &t) {
+  return 0.5f * sqrtf(t.r3.x * t.r3.x + t.r3.y * t.r3.y + t.r3.z * t.r3.z);
 }
 
-__device__ __forceinline__ Mom combine(const Mom &a, const Mom &b) {
-  Mom o;
-  const float A = a.area + b.area;
-  const float wa = A > 0.0f ? a.area / A : 0.5f, wb = 1.0f - wa;
-  o.px = wa * a.px + wb * b.px;
-  o.py = wa * a.py + wb * b.py;
-  o.pz = wa * a.pz + wb * b.pz;
-  o.area = A;
-  o.nx = a.nx + b.nx;
-  o.ny = a.ny + b.ny;
-  o.nz = a.nz + b.nz;
-  const float da[3] = {a.px - o.px, a.py - o.py, a.pz - o.pz}, db[3] = {b.px - o.px, b.py - o.py, b.pz - o.pz};
-  const float na[3] = {a.nx, a.ny, a.nz}, nb[3] = {b.nx, b.ny, b.nz};
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) o.m[3 * i + j] = a.m[3 * i + j] + b.m[3 * i + j] + na[i] * da[j] + nb[i] * db[j];
-  o.r = fmaxf(a.r + sqrtf(da[0] * da[0] + da[1] * da[1] + da[2] * da[2]),
-              b.r + sqrtf(db[0] * db[0] + db[1] * db[1] + db[2] * db[2]));
-  return o;
-}
-
-__device__ __forceinline__ void store_mom(float4 *mom, float *area, int i, const Mom &o) {
-  __stcg(mom + 4 * i + 0, make_float4(o.px, o.py, o.pz, o.r));
-  __stcg(mom + 4 * i + 1, make_float4(o.nx, o.ny, o.nz, o.m[0]));
-  __stcg(mom + 4 * i + 2, make_float4(o.m[1], o.m[2], o.m[3], o.m[4]));
-  __stcg(mom + 4 * i + 3, make_float4(o.m[5], o.m[6], o.m[7], o.m[8]));
-  __stcg(area + i, o.area);
-}
-
-__device__ __forceinline__ Mom load_mom(const float4 *mom, const float *area, int i) {
-  Mom o;
-  const float4 a = __ldcg(mom + 4 * i), b = __ldcg(mom + 4 * i + 1), c = __ldcg(mom + 4 * i + 2),
-               d = __ldcg(mom + 4 * i + 3);
-  o.px = a.x; o.py = a.y; o.pz = a.z; o.r = a.w;
-  o.nx = b.x; o.ny = b.y; o.nz = b.z; o.m[0] = b.w;
-  o.m[1] = c.x; o.m[2] = c.y; o.m[3] = c.z; o.m[4] = c.w;
-  o.m[5] = d.x; o.m[6] = d.y; o.m[7] = d.z; o.m[8] = d.w;
-  o.area = __ldcg(area + i);
-  return o;
-}
-
-__global__ __launch_bounds__(kThreads) void k_moments(int n, const TriRec *__restrict__ tris,
-                                                      const int2 *__restrict__ child, const int *__restrict__ iparent,
-                                                      const int *__restrict__ lparent, int *visits, float4 *mom,
-                                                      float *area) {
+__global__ __launch_bounds__(kThreads) void k_areas(int n, const TriRec *__restrict__ tris,
+                                                    const int2 *__restrict__ child, const int *__restrict__ iparent,
+                                                    const int *__restrict__ lparent, int *visits, float *area) {
   const int leaf = blockIdx.x * kThreads + threadIdx.x;
   if (leaf >= n) return;
   int node = lparent[leaf];
@@ -420,94 +398,90 @@ __global__ __launch_bounds__(kThreads) void k_moments(int n, const TriRec *__res
     if (atomicAdd(visits + node, 1) == 0) return;
     __threadfence();
     const int2 c = child[node];
-    const Mom a = c.x < 0 ? leaf_mom(tris[c.x & 0x7fffffff]) : load_mom(mom, area, c.x);
-    const Mom b = c.y < 0 ? leaf_mom(tris[c.y & 0x7fffffff]) : load_mom(mom, area, c.y);
-    store_mom(mom, area, node, combine(a, b));
+    const float a = c.x < 0 ? tri_area(tris[c.x & 0x7fffffff]) : __ldcg(area + c.x);
+    const float b = c.y < 0 ? tri_area(tris[c.y & 0x7fffffff]) : __ldcg(area + c.y);
+    __stcg(area + node, a + b);
     node = iparent[node];
   }
-}
-
-__global__ void k_moments_single(const TriRec *tris, float4 *mom) {
-  const Mom o = leaf_mom(tris[0]);
-  mom[0] = make_float4(o.px, o.py, o.pz, o.r);
-  mom[1] = make_float4(o.nx, o.ny, o.nz, 0.0f);
-  mom[2] = make_float4(0, 0, 0, 0);
-  mom[3] = make_float4(0, 0, 0, 0);
 }
 
 inline unsigned blocks_for(size_t n) { return static_cast<unsigned>((n + kThreads - 1) / kThreads); }
 
 }  // namespace
 
-size_t lbvh_temp_bytes(uint32_t num_tris) { return temp_layout(num_tris, nullptr, nullptr); }
+size_t lbvh_temp_bytes(uint64_t total_tris, int num_meshes) { return temp_layout(total_tris, num_meshes, nullptr, nullptr); }
 
-size_t lbvh_mesh_bytes(uint32_t T, bool with_moments) {
-  const size_t n = std::max<uint32_t>(T, 1), m = std::max<uint32_t>(T, 2) - 1;
-  return align256(n * sizeof(TriRec)) + align256(m * sizeof(Node)) + align256(n * 4) + align256(6 * 4) +
-         (with_moments ? align256(m * 4 * sizeof(float4)) : 0);
+size_t lbvh_bytes(uint64_t T, int M, bool with_areas) {
+  const size_t n = std::max<uint64_t>(T, 1), m = std::max<uint64_t>(T, 2) - 1;
+  return align256(n * sizeof(TriRec)) + align256((m + M) * sizeof(Node)) + align256(n * 4) +
+         align256(size_t(M) * 6 * 4) + (with_areas ? align256(m * sizeof(float)) : 0);
 }
 
-void lbvh_bind_mesh(MeshDev &m, void *mem, bool with_moments) {
-  const size_t n = std::max<uint32_t>(m.num_tris, 1), k = std::max<uint32_t>(m.num_tris, 2) - 1;
+void lbvh_bind(BvhDev &b, void *mem, uint64_t T, int M, bool with_areas) {
+  const size_t n = std::max<uint64_t>(T, 1), m = std::max<uint64_t>(T, 2) - 1;
   char *p = static_cast<char *>(mem);
-  m.tris = reinterpret_cast<TriRec *>(p);
+  b.tris = reinterpret_cast<TriRec *>(p);
   p += align256(n * sizeof(TriRec));
-  m.nodes = reinterpret_cast<Node *>(p);
-  p += align256(k * sizeof(Node));
-  m.leaf_order = reinterpret_cast<uint32_t *>(p);
+  b.nodes = reinterpret_cast<Node *>(p);
+  p += align256((m + M) * sizeof(Node));
+  b.leaf_order = reinterpret_cast<uint32_t *>(p);
   p += align256(n * 4);
-  m.bounds = reinterpret_cast<uint32_t *>(p);
-  p += align256(6 * 4);
-  m.moments = with_moments ? reinterpret_cast<float4 *>(p) : nullptr;
+  b.bounds = reinterpret_cast<uint32_t *>(p);
+  p += align256(size_t(M) * 6 * 4);
+  b.node_area = with_areas ? reinterpret_cast<float *>(p) : nullptr;
+  b.num_inner = T >= 2 ? static_cast<int>(T - 1) : 0;
+  b.num_nodes = b.num_inner + M;
 }
 
-cudaError_t lbvh_build(MeshDev &m, int leaf_size, void *temp, size_t temp_bytes, uint32_t *err, cudaStream_t st) {
-  const uint32_t T = m.num_tris;
-  if (T == 0) return cudaErrorInvalidValue;
+cudaError_t lbvh_build(const BatchDev &B, BvhDev &b, void *temp, size_t temp_bytes, uint32_t *err, cudaStream_t st) {
+  const uint64_t T = B.total_tris;
+  const int M = B.num_meshes;
+  if (T == 0 || M == 0) return cudaErrorInvalidValue;
+  if (T >= (1ull << 31)) return cudaErrorInvalidValue;
   BuildTemp t;
-  const size_t need = temp_layout(T, static_cast<char *>(temp), &t);
+  const size_t need = temp_layout(T, M, static_cast<char *>(temp), &t);
   if (need > temp_bytes) return cudaErrorMemoryAllocation;
-  leaf_size = std::max(1, std::min(leaf_size, 16));
-  m.leaf_size = leaf_size;
   cudaError_t e;
-  k_init_bounds<<<1, 32, 0, st>>>(m.bounds);
+  k_init_bounds<<<(6 * M + 255) / 256, 256, 0, st>>>(b.bounds, M);
   note_launch();
-  k_prep<<<blocks_for(T), kThreads, 0, st>>>(m.verts, m.idx, m.num_verts, T, t.rec, t.lo, t.hi, m.bounds, err);
+  k_prep<<<blocks_for(T), kThreads, 0, st>>>(B, t.rec, t.lo, t.hi, b.bounds, err);
   note_launch();
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  if (T == 1) {
-    k_single<<<1, 1, 0, st>>>(t.lo, t.hi, m.nodes);
-    note_launch();
-    k_gather<<<1, kThreads, 0, st>>>(1, nullptr, t.rec, m.tris, m.leaf_order);
-    note_launch();
-    if (m.moments) {
-      k_moments_single<<<1, 1, 0, st>>>(m.tris, m.moments);
-      note_launch();
-    }
-    return cudaGetLastError();
-  }
-  k_morton<<<blocks_for(T), kThreads, 0, st>>>(t.lo, t.hi, T, m.bounds, t.keys, t.vals);
-  note_launch();
-  if ((e = radix_sort_pairs(t.keys, t.vals, t.keys_alt, t.vals_alt, T, 30, Scratch{t.scratch, t.scratch_bytes}, st)) !=
-      cudaSuccess)
-    return e;
   const int n = static_cast<int>(T);
-  k_hierarchy<<<blocks_for(T - 1), kThreads, 0, st>>>(t.keys, n, t.child, t.range, t.iparent, t.lparent);
-  note_launch();
-  if ((e = cudaMemsetAsync(t.visits, 0, sizeof(int) * (T - 1), st)) != cudaSuccess) return e;
-  k_refit<<<blocks_for(T), kThreads, 0, st>>>(n, t.vals, t.lo, t.hi, t.child, t.iparent, t.lparent, t.visits, t.ilo,
-                                               t.ihi);
-  note_launch();
-  k_layout<<<blocks_for(T - 1), kThreads, 0, st>>>(n, leaf_size, t.vals, t.lo, t.hi, t.child, t.range, t.ilo, t.ihi,
-                                                    m.nodes);
-  note_launch();
-  k_gather<<<blocks_for(T), kThreads, 0, st>>>(T, t.vals, t.rec, m.tris, m.leaf_order);
-  note_launch();
-  if (m.moments) {
-    // the inner boxes are no longer needed: their space holds the node areas
+  const uint32_t *vals = nullptr;
+  if (T >= 2) {
+    k_morton<<<blocks_for(T), kThreads, 0, st>>>(B, t.lo, t.hi, b.bounds, t.keys, t.vals);
+    note_launch();
+    int mesh_bits = 0;
+    while ((1 << mesh_bits) < M) ++mesh_bits;
+    if ((e = radix_sort_pairs(t.keys, t.vals, t.keys_alt, t.vals_alt, T, 30 + mesh_bits,
+                              Scratch{t.scratch, t.scratch_bytes}, st)) != cudaSuccess)
+      return e;
+    k_hierarchy<<<blocks_for(T - 1), kThreads, 0, st>>>(t.keys, n, t.child, t.range, t.iparent, t.lparent);
+    note_launch();
+    if ((e = cudaMemsetAsync(t.subtree, 0xff, sizeof(int) * M, st)) != cudaSuccess) return e;
+    k_find_subtrees<<<blocks_for(T - 1), kThreads, 0, st>>>(B, t.keys, n, t.range, t.subtree);
+    note_launch();
     if ((e = cudaMemsetAsync(t.visits, 0, sizeof(int) * (T - 1), st)) != cudaSuccess) return e;
-    k_moments<<<blocks_for(T), kThreads, 0, st>>>(n, m.tris, t.child, t.iparent, t.lparent, t.visits, m.moments,
-                                                  reinterpret_cast<float *>(t.ilo));
+    k_refit<<<blocks_for(T), kThreads, 0, st>>>(n, t.vals, t.lo, t.hi, t.child, t.iparent, t.lparent, t.visits, t.ilo,
+                                                 t.ihi);
+    note_launch();
+    k_layout<<<blocks_for(T - 1), kThreads, 0, st>>>(B, n, t.keys, t.vals, t.lo, t.hi, t.child, t.range, t.ilo, t.ihi,
+                                                      b.nodes);
+    note_launch();
+    vals = t.vals;
+  } else {
+    // one triangle in the whole batch: its sorted position is 0
+    if ((e = cudaMemsetAsync(t.vals, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+    vals = t.vals;
+  }
+  k_roots<<<(M + 127) / 128, 128, 0, st>>>(B, b.num_inner, vals, t.lo, t.hi, t.ilo, t.ihi, t.subtree, b.nodes, err);
+  note_launch();
+  k_gather<<<blocks_for(T), kThreads, 0, st>>>(B, vals, t.rec, b.tris, b.leaf_order);
+  note_launch();
+  if (b.node_area && T >= 2) {
+    if ((e = cudaMemsetAsync(t.visits, 0, sizeof(int) * (T - 1), st)) != cudaSuccess) return e;
+    k_areas<<<blocks_for(T), kThreads, 0, st>>>(n, b.tris, t.child, t.iparent, t.lparent, t.visits, b.node_area);
     note_launch();
   }
   return cudaGetLastError();

@@ -23,20 +23,27 @@ inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 struct TriCells {
   f3 a, b, c;
   int lo[3], hi[3];
+  int mesh;
 };
 
 __device__ __forceinline__ f3 vload(const float *v, uint32_t i) {
   return {__ldg(v + 3ull * i), __ldg(v + 3ull * i + 1), __ldg(v + 3ull * i + 2)};
 }
 
-// Out-of-range indices read vertex 0 (the bake reports the mesh as bad; reads stay in bounds).
-__device__ __forceinline__ TriCells tri_cells(const float *__restrict__ verts, const uint32_t *__restrict__ idx,
-                                              uint32_t V, uint32_t t, const GridDev &g) {
+// Triangle t (global) with its mesh's clamped candidate box. Out-of-range indices read vertex 0
+// (the bake reports the mesh as bad; reads stay in bounds). A mesh without an occupancy output
+// gets an empty box.
+__device__ __forceinline__ TriCells tri_cells(const BatchDev &B, uint64_t t) {
   TriCells r;
-  const uint32_t i0 = __ldg(idx + 3ull * t), i1 = __ldg(idx + 3ull * t + 1), i2 = __ldg(idx + 3ull * t + 2);
-  r.a = vload(verts, i0 < V ? i0 : 0);
-  r.b = vload(verts, i1 < V ? i1 : 0);
-  r.c = vload(verts, i2 < V ? i2 : 0);
+  r.mesh = find_mesh(B.tri_starts, B.num_meshes, t);
+  const MeshRec &M = B.recs[r.mesh];
+  const uint64_t lt = t - B.tri_starts[r.mesh];
+  const uint32_t V = M.num_verts;
+  const uint32_t i0 = __ldg(M.idx + 3 * lt), i1 = __ldg(M.idx + 3 * lt + 1), i2 = __ldg(M.idx + 3 * lt + 2);
+  r.a = vload(M.verts, i0 < V ? i0 : 0);
+  r.b = vload(M.verts, i1 < V ? i1 : 0);
+  r.c = vload(M.verts, i2 < V ? i2 : 0);
+  const GridDev &g = M.g;
   const float mn[3] = {min_ref(min_ref(r.a.x, r.b.x), r.c.x), min_ref(min_ref(r.a.y, r.b.y), r.c.y),
                        min_ref(min_ref(r.a.z, r.b.z), r.c.z)};
   const float mx[3] = {max_ref(max_ref(r.a.x, r.b.x), r.c.x), max_ref(max_ref(r.a.y, r.b.y), r.c.y),
@@ -48,33 +55,50 @@ __device__ __forceinline__ TriCells tri_cells(const float *__restrict__ verts, c
     r.lo[k] = cell_index_clamped(mn[k], o[k], g.voxel, nmax[k]);
     r.hi[k] = cell_index_clamped(mx[k], o[k], g.voxel, nmax[k]);
   }
+  if (!M.occ) {
+    r.lo[0] = 0;
+    r.hi[0] = -1;
+  }
   return r;
 }
 
-__global__ __launch_bounds__(kThreads) void k_occ_items(const float *__restrict__ verts,
-                                                        const uint32_t *__restrict__ idx, uint32_t V, uint32_t T, GridDev g,
-                                                        uint32_t *__restrict__ items) {
-  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
-  if (t >= T) return;
-  const TriCells tc = tri_cells(verts, idx, V, t, g);
+__global__ __launch_bounds__(kThreads) void k_occ_items(BatchDev B, uint32_t *__restrict__ items) {
+  const uint64_t t = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
+  if (t >= B.total_tris) return;
+  const TriCells tc = tri_cells(B, t);
+  if (tc.hi[0] < tc.lo[0]) {
+    items[t] = 0;
+    return;
+  }
   const uint64_t n = uint64_t(tc.hi[0] - tc.lo[0] + 1) * uint64_t(tc.hi[1] - tc.lo[1] + 1) *
                      uint64_t(tc.hi[2] - tc.lo[2] + 1);
   items[t] = n > 0xffffffffull ? 0xffffffffu : static_cast<uint32_t>(n);
 }
 
+// Clears the occupancy grids of the batch (one pass over the global cells).
+__global__ __launch_bounds__(kThreads) void k_occ_clear(BatchDev B) {
+  const uint64_t stride = uint64_t(gridDim.x) * kThreads * 16;
+  for (uint64_t c0 = (uint64_t(blockIdx.x) * kThreads + threadIdx.x) * 16; c0 < B.total_cells; c0 += stride) {
+    int m = find_mesh(B.cell_starts, B.num_meshes, c0);
+    for (uint64_t c = c0; c < c0 + 16 && c < B.total_cells; ++c) {
+      while (c >= B.cell_starts[m + 1]) ++m;
+      uint8_t *occ = B.recs[m].occ;
+      if (occ) occ[c - B.cell_starts[m]] = 0;
+    }
+  }
+}
+
 template <bool FIRST>
-__global__ __launch_bounds__(kThreads) void k_occ_test(const float *__restrict__ verts,
-                                                       const uint32_t *__restrict__ idx, uint32_t V, uint32_t T, GridDev g,
-                                                       const uint64_t *__restrict__ starts, uint8_t *__restrict__ occ,
+__global__ __launch_bounds__(kThreads) void k_occ_test(BatchDev B, const uint64_t *__restrict__ starts,
                                                        uint32_t *__restrict__ first_tri,
                                                        unsigned long long *__restrict__ sat_tests) {
+  const uint64_t T = B.total_tris;
   const uint64_t total = starts[T];
   const uint64_t stride = uint64_t(gridDim.x) * kThreads * kExpandChunk;
-  const float h = __fmul_rn(g.voxel, 0.5f);
   unsigned long long tests = 0;
   for (uint64_t w0 = (uint64_t(blockIdx.x) * kThreads + threadIdx.x) * kExpandChunk; w0 < total; w0 += stride) {
-    uint32_t t = item_owner(starts, T, w0);
-    TriCells tc = tri_cells(verts, idx, V, t, g);
+    uint64_t t = item_owner(starts, static_cast<uint32_t>(T), w0);
+    TriCells tc = tri_cells(B, t);
     uint64_t tstart = starts[t], tend = starts[t + 1];
     const uint64_t wend = min(w0 + kExpandChunk, total);
     for (uint64_t w = w0; w < wend; ++w) {
@@ -82,8 +106,10 @@ __global__ __launch_bounds__(kThreads) void k_occ_test(const float *__restrict__
         ++t;
         tstart = tend;
         tend = starts[t + 1];
-        if (tend > tstart) tc = tri_cells(verts, idx, V, t, g);
+        if (tend > tstart) tc = tri_cells(B, t);
       }
+      const MeshRec &M = B.recs[tc.mesh];
+      const GridDev &g = M.g;
       const uint64_t k = w - tstart;
       const uint32_t sx = tc.hi[0] - tc.lo[0] + 1, sy = tc.hi[1] - tc.lo[1] + 1;
       const int x = tc.lo[0] + static_cast<int>(k % sx);
@@ -91,10 +117,10 @@ __global__ __launch_bounds__(kThreads) void k_occ_test(const float *__restrict__
       const int z = tc.lo[2] + static_cast<int>(k / (uint64_t(sx) * sy));
       const f3 c = {cell_center(g.ox, x, g.voxel), cell_center(g.oy, y, g.voxel), cell_center(g.oz, z, g.voxel)};
       ++tests;
-      if (sat_overlap(c, h, tc.a, tc.b, tc.c)) {
+      if (sat_overlap(c, __fmul_rn(g.voxel, 0.5f), tc.a, tc.b, tc.c)) {
         const uint64_t cell = (uint64_t(z) * g.ny + y) * g.nx + x;
-        occ[cell] = 1;
-        if (FIRST) atomicMin(first_tri + cell, t);
+        M.occ[cell] = 1;
+        if (FIRST) atomicMin(first_tri + cell, static_cast<uint32_t>(t - B.tri_starts[tc.mesh]));
       }
     }
   }
@@ -112,7 +138,7 @@ struct OccTemp {
   size_t scratch_bytes;
 };
 
-size_t occ_layout(uint32_t T, char *base, OccTemp *o) {
+size_t occ_layout(uint64_t T, char *base, OccTemp *o) {
   size_t off = 0;
   auto take = [&](size_t bytes) {
     char *p = base ? base + off : nullptr;
@@ -128,41 +154,35 @@ size_t occ_layout(uint32_t T, char *base, OccTemp *o) {
   return off;
 }
 
-template <bool FIRST>
-cudaError_t occ_run(const float *verts, const uint32_t *idx, uint32_t V, uint32_t T, GridDev g, uint8_t *occ, uint32_t *first,
-                    void *temp, size_t temp_bytes, unsigned long long *sat_tests, cudaStream_t st) {
-  const size_t cells = size_t(g.nx) * g.ny * g.nz;
-  cudaError_t e = cudaMemsetAsync(occ, 0, cells, st);
-  if (e != cudaSuccess) return e;
-  if (FIRST && (e = cudaMemsetAsync(first, 0xff, cells * 4, st)) != cudaSuccess) return e;
-  if (T == 0) return cudaSuccess;
-  OccTemp o;
-  if (occ_layout(T, static_cast<char *>(temp), &o) > temp_bytes) return cudaErrorMemoryAllocation;
-  k_occ_items<<<(T + kThreads - 1) / kThreads, kThreads, 0, st>>>(verts, idx, V, T, g, o.items);
-  note_launch();
-  if ((e = exclusive_scan_u32(o.items, o.starts, T, Scratch{o.scratch, o.scratch_bytes}, st)) != cudaSuccess) return e;
-  int dev = 0, sms = 148;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  k_occ_test<FIRST><<<sms * 8, kThreads, 0, st>>>(verts, idx, V, T, g, o.starts, occ, first, sat_tests);
-  note_launch();
-  return cudaGetLastError();
-}
-
 }  // namespace
 
-size_t occupancy_temp_bytes(uint32_t num_tris) { return occ_layout(num_tris, nullptr, nullptr); }
+size_t occupancy_temp_bytes(uint64_t total_tris) { return occ_layout(total_tris, nullptr, nullptr); }
 
-cudaError_t occupancy_dense(const float *verts, const uint32_t *idx, uint32_t num_verts, uint32_t num_tris, GridDev g,
-                            uint8_t *occ, void *temp, size_t temp_bytes, unsigned long long *sat_tests,
-                            cudaStream_t st) {
-  return occ_run<false>(verts, idx, num_verts, num_tris, g, occ, nullptr, temp, temp_bytes, sat_tests, st);
-}
-
-cudaError_t occupancy_dense_first(const float *verts, const uint32_t *idx, uint32_t num_verts, uint32_t num_tris,
-                                  GridDev g, uint8_t *occ, uint32_t *first_tri, void *temp, size_t temp_bytes,
-                                  cudaStream_t st) {
-  return occ_run<true>(verts, idx, num_verts, num_tris, g, occ, first_tri, temp, temp_bytes, nullptr, st);
+cudaError_t occupancy_batch(const BatchDev &B, uint32_t *first_tri, void *temp, size_t temp_bytes,
+                            unsigned long long *sat_tests, int num_sms, cudaStream_t st) {
+  const uint64_t T = B.total_tris;
+  cudaError_t e;
+  if (B.total_cells) {
+    const uint64_t blocks = std::min<uint64_t>((B.total_cells + kThreads * 16 - 1) / (kThreads * 16), uint64_t(num_sms) * 16);
+    k_occ_clear<<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(B);
+    note_launch();
+  }
+  if (first_tri) {
+    if (B.num_meshes != 1) return cudaErrorInvalidValue;
+    if ((e = cudaMemsetAsync(first_tri, 0xff, B.total_cells * 4, st)) != cudaSuccess) return e;
+  }
+  if (T == 0) return cudaGetLastError();
+  OccTemp o;
+  if (occ_layout(T, static_cast<char *>(temp), &o) > temp_bytes) return cudaErrorMemoryAllocation;
+  k_occ_items<<<static_cast<unsigned>((T + kThreads - 1) / kThreads), kThreads, 0, st>>>(B, o.items);
+  note_launch();
+  if ((e = exclusive_scan_u32(o.items, o.starts, T, Scratch{o.scratch, o.scratch_bytes}, st)) != cudaSuccess) return e;
+  if (first_tri)
+    k_occ_test<true><<<num_sms * 8, kThreads, 0, st>>>(B, o.starts, first_tri, sat_tests);
+  else
+    k_occ_test<false><<<num_sms * 8, kThreads, 0, st>>>(B, o.starts, nullptr, sat_tests);
+  note_launch();
+  return cudaGetLastError();
 }
 
 }  // namespace sdfb

@@ -32,7 +32,7 @@ inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 struct TriCols {
   f3 a, b, c;
   int x0, x1, y0, y1;
-  bool ok;
+  int mesh;
 };
 
 __device__ __forceinline__ f3 vload(const float *v, uint32_t i) {
@@ -49,46 +49,48 @@ __device__ __forceinline__ void col_range(float mn, float mx, float o, float v, 
   hi = fb < 0.0f ? -1 : (fb > float(n - 1) ? n - 1 : static_cast<int>(fb));
 }
 
-__device__ __forceinline__ TriCols tri_cols(const float *__restrict__ verts, const uint32_t *__restrict__ idx,
-                                            uint32_t V, uint32_t t, const GridDev &g) {
+// Parity triangle t (global over the parity meshes) and its candidate columns.
+__device__ __forceinline__ TriCols tri_cols(const BatchDev &B, uint64_t t) {
   TriCols r;
-  const uint32_t i0 = __ldg(idx + 3ull * t), i1 = __ldg(idx + 3ull * t + 1), i2 = __ldg(idx + 3ull * t + 2);
-  r.a = vload(verts, i0 < V ? i0 : 0);
-  r.b = vload(verts, i1 < V ? i1 : 0);
-  r.c = vload(verts, i2 < V ? i2 : 0);
-  r.ok = isfinite(r.a.x + r.a.y + r.b.x + r.b.y + r.c.x + r.c.y + r.a.z + r.b.z + r.c.z);
+  r.mesh = find_mesh(B.ptri_starts, B.num_meshes, t);
+  const MeshRec &M = B.recs[r.mesh];
+  const uint64_t lt = t - B.ptri_starts[r.mesh];
+  const uint32_t V = M.pnum_verts;
+  const uint32_t i0 = __ldg(M.pidx + 3 * lt), i1 = __ldg(M.pidx + 3 * lt + 1), i2 = __ldg(M.pidx + 3 * lt + 2);
+  r.a = vload(M.pverts, i0 < V ? i0 : 0);
+  r.b = vload(M.pverts, i1 < V ? i1 : 0);
+  r.c = vload(M.pverts, i2 < V ? i2 : 0);
+  const bool ok = isfinite(r.a.x + r.a.y + r.b.x + r.b.y + r.c.x + r.c.y + r.a.z + r.b.z + r.c.z);
+  const GridDev &g = M.g;
   col_range(fminf(fminf(r.a.x, r.b.x), r.c.x), fmaxf(fmaxf(r.a.x, r.b.x), r.c.x), g.ox, g.voxel, g.nx, r.x0, r.x1);
   col_range(fminf(fminf(r.a.y, r.b.y), r.c.y), fmaxf(fmaxf(r.a.y, r.b.y), r.c.y), g.oy, g.voxel, g.ny, r.y0, r.y1);
-  if (!r.ok || r.x1 < r.x0 || r.y1 < r.y0) {
+  if (!ok || r.x1 < r.x0 || r.y1 < r.y0) {
     r.x0 = r.y0 = 0;
     r.x1 = r.y1 = -1;
   }
   return r;
 }
 
-__global__ __launch_bounds__(kThreads) void k_col_items(const float *__restrict__ verts,
-                                                        const uint32_t *__restrict__ idx, uint32_t V, uint32_t T,
-                                                        GridDev g, uint32_t *__restrict__ items) {
-  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
-  if (t >= T) return;
-  const TriCols tc = tri_cols(verts, idx, V, t, g);
+__global__ __launch_bounds__(kThreads) void k_col_items(BatchDev B, uint32_t *__restrict__ items) {
+  const uint64_t t = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
+  if (t >= B.total_ptris) return;
+  const TriCols tc = tri_cols(B, t);
   const uint64_t n = uint64_t(tc.x1 - tc.x0 + 1) * uint64_t(tc.y1 - tc.y0 + 1);
   items[t] = tc.x1 < tc.x0 ? 0u : (n > 0xffffffffull ? 0xffffffffu : static_cast<uint32_t>(n));
 }
 
 template <bool FILL>
-__global__ __launch_bounds__(kThreads) void k_col_hits(const float *__restrict__ verts,
-                                                       const uint32_t *__restrict__ idx, uint32_t V, uint32_t T,
-                                                       GridDev g, const uint64_t *__restrict__ starts,
+__global__ __launch_bounds__(kThreads) void k_col_hits(BatchDev B, const uint64_t *__restrict__ starts,
                                                        uint32_t *__restrict__ col_count,
                                                        const uint64_t *__restrict__ col_start,
-                                                       float *__restrict__ col_z, uint64_t capacity,
-                                                       uint32_t *__restrict__ err) {
+                                                       float *__restrict__ col_z, int8_t *__restrict__ col_s,
+                                                       uint64_t capacity, uint32_t *__restrict__ err) {
+  const uint64_t T = B.total_ptris;
   const uint64_t total = starts[T];
   const uint64_t stride = uint64_t(gridDim.x) * kThreads * kExpandChunk;
   for (uint64_t w0 = (uint64_t(blockIdx.x) * kThreads + threadIdx.x) * kExpandChunk; w0 < total; w0 += stride) {
-    uint32_t t = item_owner(starts, T, w0);
-    TriCols tc = tri_cols(verts, idx, V, t, g);
+    uint64_t t = item_owner(starts, static_cast<uint32_t>(T), w0);
+    TriCols tc = tri_cols(B, t);
     uint64_t tstart = starts[t], tend = starts[t + 1];
     const uint64_t wend = min(w0 + kExpandChunk, total);
     for (uint64_t w = w0; w < wend; ++w) {
@@ -96,21 +98,28 @@ __global__ __launch_bounds__(kThreads) void k_col_hits(const float *__restrict__
         ++t;
         tstart = tend;
         tend = starts[t + 1];
-        if (tend > tstart) tc = tri_cols(verts, idx, V, t, g);
+        if (tend > tstart) tc = tri_cols(B, t);
       }
+      const MeshRec &M = B.recs[tc.mesh];
+      const GridDev &g = M.g;
       const uint64_t k = w - tstart;
       const uint32_t sx = tc.x1 - tc.x0 + 1;
       const int x = tc.x0 + static_cast<int>(k % sx);
       const int y = tc.y0 + static_cast<int>(k / sx);
       const float px = cell_center(g.ox, x, g.voxel), py = cell_center(g.oy, y, g.voxel);
       float z;
-      if (!column_crossing(tc.a, tc.b, tc.c, px, py, z)) continue;
-      const uint64_t col = uint64_t(y) * g.nx + x;
+      int sgn;
+      if (!column_crossing(tc.a, tc.b, tc.c, px, py, z, sgn)) continue;
+      const uint64_t col = M.col_base + uint64_t(y) * g.nx + x;
       const uint32_t slot = atomicAdd(col_count + col, 1u);
       if (FILL) {
         const uint64_t at = col_start[col] + slot;
-        if (at < capacity) col_z[at] = z;
-        else atomic_or_err(err, kErrCrossingOverflow);
+        if (at < capacity) {
+          col_z[at] = z;
+          col_s[at] = static_cast<int8_t>(sgn);
+        } else {
+          atomic_or_err(err, kErrCrossingOverflow);
+        }
       }
     }
   }
@@ -124,7 +133,7 @@ struct ParTemp {
   size_t scratch_bytes;
 };
 
-size_t par_layout(uint32_t T, size_t ncols, char *base, ParTemp *o) {
+size_t par_layout(uint64_t T, uint64_t ncols, char *base, ParTemp *o) {
   size_t off = 0;
   auto take = [&](size_t bytes) {
     char *p = base ? base + off : nullptr;
@@ -143,33 +152,28 @@ size_t par_layout(uint32_t T, size_t ncols, char *base, ParTemp *o) {
 
 }  // namespace
 
-size_t parity_temp_bytes(uint32_t num_tris, int nx, int ny) {
-  return par_layout(num_tris, size_t(nx) * ny, nullptr, nullptr);
+size_t parity_temp_bytes(uint64_t total_ptris, uint64_t total_cols) {
+  return par_layout(total_ptris, total_cols, nullptr, nullptr);
 }
 
-cudaError_t parity_columns(const float *verts, const uint32_t *idx, uint32_t V, uint32_t T, GridDev g,
-                           uint64_t *col_start, float *col_z, uint64_t capacity, void *temp, size_t temp_bytes,
-                           uint32_t *err, cudaStream_t st) {
-  const size_t ncols = size_t(g.nx) * g.ny;
+cudaError_t parity_columns(const BatchDev &B, uint64_t *col_start, float *col_z, int8_t *col_s, uint64_t capacity,
+                           void *temp, size_t temp_bytes, uint32_t *err, int num_sms, cudaStream_t st) {
+  const uint64_t T = B.total_ptris, ncols = B.total_cols;
   ParTemp o;
   if (par_layout(T, ncols, static_cast<char *>(temp), &o) > temp_bytes) return cudaErrorMemoryAllocation;
   cudaError_t e;
   if ((e = cudaMemsetAsync(o.col_count, 0, ncols * 4, st)) != cudaSuccess) return e;
   if (T == 0) return cudaMemsetAsync(col_start, 0, (ncols + 1) * 8, st);
   const Scratch sc{o.scratch, o.scratch_bytes};
-  k_col_items<<<(T + kThreads - 1) / kThreads, kThreads, 0, st>>>(verts, idx, V, T, g, o.items);
+  k_col_items<<<static_cast<unsigned>((T + kThreads - 1) / kThreads), kThreads, 0, st>>>(B, o.items);
   note_launch();
   if ((e = exclusive_scan_u32(o.items, o.starts, T, sc, st)) != cudaSuccess) return e;
-  int dev = 0, sms = 148;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const unsigned grid = sms * 8;
-  k_col_hits<false><<<grid, kThreads, 0, st>>>(verts, idx, V, T, g, o.starts, o.col_count, nullptr, nullptr, 0, err);
+  const unsigned grid = num_sms * 8;
+  k_col_hits<false><<<grid, kThreads, 0, st>>>(B, o.starts, o.col_count, nullptr, nullptr, nullptr, 0, err);
   note_launch();
   if ((e = exclusive_scan_u32(o.col_count, col_start, ncols, sc, st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(o.col_count, 0, ncols * 4, st)) != cudaSuccess) return e;
-  k_col_hits<true><<<grid, kThreads, 0, st>>>(verts, idx, V, T, g, o.starts, o.col_count, col_start, col_z, capacity,
-                                              err);
+  k_col_hits<true><<<grid, kThreads, 0, st>>>(B, o.starts, o.col_count, col_start, col_z, col_s, capacity, err);
   note_launch();
   return cudaGetLastError();
 }

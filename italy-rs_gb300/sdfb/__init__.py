@@ -51,21 +51,22 @@ class GridDesc(C.Structure):
 class Opts(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("sign_mode", C.c_int32), ("band_voxels", C.c_float),
                 ("leaf_size", C.c_int32), ("tile", C.c_int32), ("no_occupancy", C.c_int32),
-                ("no_distance", C.c_int32), ("count_work", C.c_int32), ("reserved", C.c_int32 * 8)]
+                ("no_distance", C.c_int32), ("count_work", C.c_int32), ("stack_depth", C.c_int32),
+                ("reserved", C.c_int32 * 7)]
 
 
 class Stats(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("sign_mode_used", C.c_int32), ("watertight", C.c_int32),
-                ("leaf_size_used", C.c_int32), ("tile_used", C.c_int32), ("pad0", C.c_int32),
+                ("leaf_size_used", C.c_int32), ("tile_used", C.c_int32), ("stack_used", C.c_int32),
                 ("ms_total", C.c_double), ("ms_prepare", C.c_double), ("ms_build", C.c_double),
                 ("ms_occupancy", C.c_double), ("ms_sign", C.c_double), ("ms_distance", C.c_double),
                 ("voxels", C.c_uint64), ("triangles", C.c_uint64), ("sat_tests", C.c_uint64),
                 ("crossings", C.c_uint64), ("box_tests", C.c_uint64), ("tri_tests", C.c_uint64),
                 ("flops_distance", C.c_double), ("kernel_launches", C.c_uint64), ("gwn_fp64_cells", C.c_uint64),
-                ("reserved", C.c_uint64 * 3)]
+                ("graph_replayed", C.c_uint64), ("reserved", C.c_uint64 * 2)]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "pad0", "struct_size")}
+        return {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "struct_size")}
 
 
 class MeshDesc(C.Structure):
@@ -160,7 +161,9 @@ def make_grid(origin, voxel, n) -> GridDesc:
 
 
 def make_opts(sign_mode: int = SIGN_AUTO, band_voxels: float = 1.0, leaf_size: int = 0, tile: int = 0,
-              no_occupancy: bool = False, no_distance: bool = False, count_work: bool = False) -> Opts:
+              no_occupancy: bool = False, no_distance: bool = False, count_work: bool = False,
+              stack_depth: int = 0) -> Opts:
+    """tile: shape 1..6 (0 = tuned); leaf_size 1..16 (0 = tuned); stack_depth 32 or 64 (0 = tuned)."""
     o = Opts()
     o.struct_size = C.sizeof(Opts)
     o.sign_mode = sign_mode
@@ -170,6 +173,7 @@ def make_opts(sign_mode: int = SIGN_AUTO, band_voxels: float = 1.0, leaf_size: i
     o.no_occupancy = int(no_occupancy)
     o.no_distance = int(no_distance)
     o.count_work = int(count_work)
+    o.stack_depth = stack_depth
     return o
 
 
@@ -295,6 +299,49 @@ class Context:
             if cnt.value <= cap:
                 return cells[:cnt.value].copy(), o, float(np.float32(v.value))
             cap = int(cnt.value)
+
+    def bake_batch(self, meshes, grids, opts: Opts | None = None, want_dist=True, want_occ=True,
+                   stats: Stats | None = None, out=None):
+        """Host-buffer batched bake of [(verts, idx), ...] onto [GridDesc, ...]. Returns
+        ([dist], [occ]); `out` may pass preallocated (dists, occs) lists (pinned memory is fastest)."""
+        n = len(meshes)
+        vs = [_f32(v).reshape(-1, 3) for v, _ in meshes]
+        fs = [_u32a(f).reshape(-1, 3) for _, f in meshes]
+        descs = (MeshDesc * n)()
+        for k in range(n):
+            descs[k].verts = vs[k].ctypes.data
+            descs[k].idx = fs[k].ctypes.data
+            descs[k].num_verts = len(vs[k])
+            descs[k].num_tris = len(fs[k])
+        gs = (GridDesc * n)(*grids)
+        if out is not None:
+            dists, occs = out
+        else:
+            dists = [np.empty(g.shape, np.float32) for g in grids] if want_dist else None
+            occs = [np.empty(g.shape, np.uint8) for g in grids] if want_occ else None
+        dp = (C.c_void_p * n)(*[d.ctypes.data for d in dists]) if dists is not None else None
+        op = (C.c_void_p * n)(*[o.ctypes.data for o in occs]) if occs is not None else None
+        st = self.lib.sdfb_bake_batch(self.h, n, descs, gs, C.byref(opts) if opts is not None else None, dp, op,
+                                      C.byref(stats) if stats is not None else None)
+        self._check(st)
+        return dists, occs
+
+    def bake_batch_device(self, dev_meshes, grids, opts: Opts | None, dist_ptrs, occ_ptrs, stream: int = 0,
+                          stats: Stats | None = None):
+        """dev_meshes: [(verts_ptr, num_verts, idx_ptr, num_tris)]; pointers are device addresses."""
+        n = len(dev_meshes)
+        descs = (MeshDesc * n)()
+        for k, (vp, nv, ip, nt) in enumerate(dev_meshes):
+            descs[k].verts = vp
+            descs[k].idx = ip
+            descs[k].num_verts = nv
+            descs[k].num_tris = nt
+        gs = (GridDesc * n)(*grids)
+        dp = (C.c_void_p * n)(*dist_ptrs) if dist_ptrs is not None else None
+        op = (C.c_void_p * n)(*occ_ptrs) if occ_ptrs is not None else None
+        st = self.lib.sdfb_bake_batch_device(self.h, n, descs, gs, C.byref(opts) if opts is not None else None, dp, op,
+                                             C.c_void_p(stream), C.byref(stats) if stats is not None else None)
+        self._check(st)
 
     def device_bytes(self) -> int:
         return int(self.lib.sdfb_ctx_device_bytes(self.h))

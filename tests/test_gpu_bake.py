@@ -135,8 +135,8 @@ def test_leaf_sizes_and_tiles_agree(ctx, golden, leaf):
     import sdfb
     v, i = golden["c1_verts"], golden["c1_idx"]
     g = sdfb.make_grid((-0.5,) * 3, 1.0 / 48, (48, 40, 36))
-    ref_d, ref_o = ctx.bake(v, i, g, sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY, leaf_size=1, tile=0))
-    for tile in range(6):
+    ref_d, ref_o = ctx.bake(v, i, g, sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY, leaf_size=1, tile=1))
+    for tile in range(1, 7):
         d, o = ctx.bake(v, i, g, sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY, leaf_size=leaf, tile=tile))
         assert np.array_equal(o, ref_o)
         # the same nearest triangle whichever way the tree is walked (a culling decision taken on an
