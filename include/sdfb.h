@@ -196,6 +196,48 @@ sdfb_status sdfb_bake_batch_device(sdfb_ctx *ctx, uint32_t count, const sdfb_mes
                                    const sdfb_grid_desc *grids, const sdfb_opts *opts, float *const *dist_outs,
                                    uint8_t *const *occ_outs, void *stream, sdfb_stats *stats);
 
+/* ---- serving ------------------------------------------------------------------------------- */
+
+typedef struct sdfb_server sdfb_server;
+
+typedef struct sdfb_server_opts {
+  uint32_t struct_size;
+  uint64_t hbm_budget_bytes; /* admission budget for resident meshes + in-flight jobs */
+  int32_t max_inflight;      /* jobs on the device at once, default 64 */
+  int32_t wave_voxels_log2;  /* work per wave (log2 voxels), default 25 */
+  int32_t reserved[8];
+} sdfb_server_opts;
+
+typedef struct sdfb_request_info {
+  uint32_t struct_size;
+  int32_t status;        /* sdfb_status of the finished request */
+  double t_submit_ms;    /* host monotonic clock */
+  double t_admit_ms;
+  double t_done_ms;
+  uint64_t voxels;
+  int32_t mesh_was_resident;
+  int32_t pad;
+} sdfb_request_info;
+
+/* Starts the serving loop (one admission/scheduling thread) on ctx's device. */
+sdfb_status sdfb_server_create(sdfb_ctx *ctx, const sdfb_server_opts *opts, sdfb_server **out);
+/* Drains in-flight work and stops the loop. */
+void sdfb_server_destroy(sdfb_server *srv);
+/* Uploads a mesh and builds its hierarchy on the device; *mesh_id identifies it from then on.
+ * Registering identical contents again returns the resident id (content hash). */
+sdfb_status sdfb_mesh_register(sdfb_server *srv, const float *verts, uint32_t num_verts, const uint32_t *idx,
+                               uint32_t num_tris, uint64_t *mesh_id);
+/* Queues a bake of a registered mesh. Output buffers are host memory owned by the caller and
+ * must stay valid until sdfb_poll reports the request done. */
+sdfb_status sdfb_submit(sdfb_server *srv, uint64_t mesh_id, const sdfb_grid_desc *grid, const sdfb_opts *opts,
+                        float *dist_out, uint8_t *occ_out, uint64_t *request_id);
+/* Waits up to timeout_ms (0 = just look, < 0 = forever) for a request. *done = 1 when finished,
+ * with its outcome in info (optional). A finished request is forgotten after it is reported. */
+sdfb_status sdfb_poll(sdfb_server *srv, uint64_t request_id, int32_t timeout_ms, int32_t *done,
+                      sdfb_request_info *info);
+/* Text of the server's last error. */
+const char *sdfb_server_last_error(const sdfb_server *srv);
+
 #ifdef __cplusplus
 }
 #endif

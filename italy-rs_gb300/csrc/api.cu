@@ -70,32 +70,23 @@ void PinBuf::release() {
 }
 
 sdfb_ctx::~sdfb_ctx() {
-  if (graph) cudaGraphExecDestroy(graph);
-  for (auto &e : ev)
-    if (e) cudaEventDestroy(e);
   if (stream) cudaStreamDestroy(stream);
 }
 
 DevBuf *sdfb_ctx::all_bufs(int i) {
-  DevBuf *b[] = {&in_verts, &in_idx,    &in_verts2, &in_idx2,   &in_caps,  &in_capidx, &out_dist,
-                 &out_occ,  &first_tri, &batch_buf, &bvh,       &build_tmp, &par_tmp,  &col_start,
-                 &col_z,    &col_s,     &caps_bvh,  &caps_tmp,  &misc,     &gwn_tmp};
+  DevBuf *b[] = {&in_verts, &in_idx,   &in_verts2, &in_idx2,    &in_caps,   &in_capidx,
+                 &out_dist, &out_occ,  &first_tri, &sparse_tmp, &sparse_out};
   return i < int(sizeof b / sizeof b[0]) ? b[i] : nullptr;
 }
 
 void sdfb_ctx::release_all() {
-  if (graph) {
-    cudaGraphExecDestroy(graph);
-    graph = nullptr;
-    graph_key.clear();
-  }
   for (int i = 0; DevBuf *b = all_bufs(i); ++i) b->release();
-  staging.release();
-  staging_out.release();
+  ws.release();
+  staging_small.release();
 }
 
 uint64_t sdfb_ctx::device_bytes() const {
-  uint64_t s = 0;
+  uint64_t s = ws.bytes();
   for (int i = 0; const DevBuf *b = const_cast<sdfb_ctx *>(this)->all_bufs(i); ++i) s += b->cap;
   return s;
 }
@@ -241,11 +232,10 @@ sdfb_status sdfb_ctx_create(int32_t device, sdfb_ctx **out) {
     delete ctx;
     return SDFB_ERR_CUDA;
   }
-  for (auto &e : ctx->ev)
-    if (cudaEventCreate(&e) != cudaSuccess) {
-      delete ctx;
-      return SDFB_ERR_CUDA;
-    }
+  if (!ctx->ws.init()) {
+    delete ctx;
+    return SDFB_ERR_CUDA;
+  }
   load_tuning(ctx);
   *out = ctx;
   return SDFB_OK;
@@ -520,7 +510,7 @@ sdfb_status sdfb_voxelize_sparse(sdfb_ctx *ctx, const float *positions, uint32_t
   ENSURE(ctx->in_idx, size_t(V) * 4);
   ENSURE(ctx->out_occ, cells);
   ENSURE(ctx->first_tri, cells * 4);
-  ENSURE(ctx->build_tmp, occupancy_temp_bytes(num_tris));
+  ENSURE(ctx->sparse_tmp, std::max(occupancy_temp_bytes(num_tris), sparse_temp_bytes(cells, 0)));
   CK(cudaMemcpyAsync(ctx->in_verts.p, positions, size_t(V) * 12, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(ctx->in_idx.p, ident.data(), size_t(V) * 4, cudaMemcpyHostToDevice, st));
   // a batch of one mesh with an occupancy output only
@@ -536,15 +526,15 @@ sdfb_status sdfb_voxelize_sparse(sdfb_ctx *ctx, const float *positions, uint32_t
   const uint64_t tables[2][2] = {{0, num_tris}, {0, cells}};
   const uint64_t zero[2] = {0, 0};
   const size_t bytes = 256 * 4;
-  ENSURE(ctx->batch_buf, bytes);
-  if (!ctx->staging.ensure(bytes)) return ctx_fail(ctx, SDFB_ERR_OUT_OF_MEMORY, "pinned staging");
-  char *hs = static_cast<char *>(ctx->staging.p);
+  ENSURE(ctx->sparse_out, bytes);
+  if (!ctx->staging_small.ensure(bytes)) return ctx_fail(ctx, SDFB_ERR_OUT_OF_MEMORY, "pinned staging");
+  char *hs = static_cast<char *>(ctx->staging_small.p);
   std::memcpy(hs, &r, sizeof r);
   std::memcpy(hs + 256, tables[0], 16);
   std::memcpy(hs + 512, tables[1], 16);
   std::memcpy(hs + 768, zero, 16);
-  CK(cudaMemcpyAsync(ctx->batch_buf.p, hs, bytes, cudaMemcpyHostToDevice, st));
-  char *d = static_cast<char *>(ctx->batch_buf.p);
+  CK(cudaMemcpyAsync(ctx->sparse_out.p, hs, bytes, cudaMemcpyHostToDevice, st));
+  char *d = static_cast<char *>(ctx->sparse_out.p);
   BatchDev B;
   B.num_meshes = 1;
   B.recs = reinterpret_cast<const MeshRec *>(d);
@@ -553,22 +543,22 @@ sdfb_status sdfb_voxelize_sparse(sdfb_ctx *ctx, const float *positions, uint32_t
   B.ptri_starts = B.tile_starts = B.gwn_tile_starts = reinterpret_cast<const uint64_t *>(d + 768);
   B.total_tris = num_tris;
   B.total_cells = cells;
-  CK(occupancy_batch(B, static_cast<uint32_t *>(ctx->first_tri.p), ctx->build_tmp.p, ctx->build_tmp.cap, nullptr,
+  CK(occupancy_batch(B, static_cast<uint32_t *>(ctx->first_tri.p), ctx->sparse_tmp.p, ctx->sparse_tmp.cap, nullptr,
                      ctx->num_sms, st));
-  ENSURE(ctx->par_tmp, sparse_temp_bytes(cells, 0));
   uint64_t total = 0;
-  CK(sparse_count(static_cast<const uint8_t *>(ctx->out_occ.p), cells, ctx->par_tmp.p, ctx->par_tmp.cap, &total, st));
+  CK(sparse_count(static_cast<const uint8_t *>(ctx->out_occ.p), cells, ctx->sparse_tmp.p, ctx->sparse_tmp.cap, &total,
+                  st));
   *count = total;
   if (total == 0) return SDFB_OK;
-  ENSURE(ctx->par_tmp, sparse_temp_bytes(cells, total));
-  ENSURE(ctx->col_z, total * 4);
+  ENSURE(ctx->sparse_tmp, sparse_temp_bytes(cells, total));
+  ENSURE(ctx->out_dist, total * 4);
   int bits = 1;
   while (bits < 32 && (uint64_t(1) << bits) < num_tris) ++bits;
   CK(sparse_emit(static_cast<const uint8_t *>(ctx->out_occ.p), static_cast<const uint32_t *>(ctx->first_tri.p), cells,
-                 total, bits, ctx->par_tmp.p, ctx->par_tmp.cap, static_cast<uint32_t *>(ctx->col_z.p), st));
+                 total, bits, ctx->sparse_tmp.p, ctx->sparse_tmp.cap, static_cast<uint32_t *>(ctx->out_dist.p), st));
   const uint64_t n = std::min<uint64_t>(total, cap);
   std::vector<uint32_t> lin(n);
-  if (n) CK(cudaMemcpyAsync(lin.data(), ctx->col_z.p, n * 4, cudaMemcpyDeviceToHost, st));
+  if (n) CK(cudaMemcpyAsync(lin.data(), ctx->out_dist.p, n * 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   const uint64_t rr = uint64_t(resolution);
   for (uint64_t i = 0; i < n; ++i) {

@@ -34,6 +34,15 @@ struct PinBuf {
   void release();
 };
 
+// A mesh hierarchy resident in device memory (built once, reused by later bakes).
+struct ResidentBvh {
+  const sdfb::Node *nodes = nullptr;
+  const sdfb::TriRec *tris = nullptr;
+  const uint32_t *leaf_order = nullptr;
+  const float *node_area = nullptr;
+  int num_nodes = 0, num_inner = 0, num_tris = 0, root = 0;
+};
+
 // One mesh of a bake as the orchestrator sees it (every pointer is device memory).
 struct PlanMesh {
   const float *verts = nullptr;   // geometry: BVH, occupancy, distance
@@ -51,6 +60,8 @@ struct PlanMesh {
   float *dist = nullptr;
   uint8_t *occ = nullptr;
   int watertight = -1;
+  const ResidentBvh *bvh = nullptr;   // set: use this hierarchy instead of building one
+  const ResidentBvh *caps = nullptr;  // set: the caps hierarchy of a resident winding-number mesh
 };
 
 // Host-side result of capping a mesh for the winding-number sign.
@@ -68,31 +79,44 @@ struct GwnInput {
   const uint64_t *col_start;
   const float *col_z;
   const int8_t *col_s;
-  sdfb::BvhDev caps;
-  uint64_t cap_total_tris;
   float band_voxels;
   uint32_t *err;
   uint64_t gwn_cells;  // cells of the winding-number meshes (refine list capacity)
 };
 
-struct GraphEntry;
+// Device workspace of one bake in flight. The context owns one; the serving loop owns one per
+// stream so consecutive waves overlap.
+struct Workspace {
+  DevBuf batch_buf, bvh, build_tmp, par_tmp, col_start, col_z, col_s, caps_bvh, caps_tmp, misc, gwn_tmp;
+  PinBuf staging;
+  cudaEvent_t ev[8] = {};
+  uint64_t col_capacity_hint = 0;
+  cudaGraphExec_t graph = nullptr;  // the last batch's launch sequence, replayed while it repeats
+  std::vector<uint8_t> graph_key;
+  uint64_t graph_launches = 0;
+  bool init();
+  ~Workspace();
+  void release();
+  uint64_t bytes() const;
+};
+
+// What enqueue_batch leaves for finish_batch.
+struct BatchState {
+  uint64_t capacity = 0, total_cols = 0, total_cells = 0, total_tris = 0, launched = 0;
+  bool any_cross = false, any_gwn = false, graphed = false;
+  int tile_id = 0, stack = 64, leaf0 = 0;
+};
+
 
 struct sdfb_ctx {
   int device = 0, num_sms = 0;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev[8] = {};
   std::string err;
   // inputs / outputs of host-buffer calls
-  DevBuf in_verts, in_idx, in_verts2, in_idx2, in_caps, in_capidx, out_dist, out_occ, first_tri;
-  // workspace of one bake
-  DevBuf batch_buf, bvh, build_tmp, par_tmp, col_start, col_z, col_s, caps_bvh, caps_tmp, misc, gwn_tmp;
-  PinBuf staging, staging_out;
-  uint64_t col_capacity_hint = 0;
-  uint64_t gwn_refined = 0;  // cells of the last bake that took the FP64 winding-number pass
-  // CUDA graph of the last batch shape (replayed when the same batch comes again)
-  cudaGraphExec_t graph = nullptr;
-  std::vector<uint8_t> graph_key;
-  uint64_t graph_launches = 0;  // kernels inside the cached graph
+  DevBuf in_verts, in_idx, in_verts2, in_idx2, in_caps, in_capidx, out_dist, out_occ, first_tri, sparse_tmp,
+      sparse_out;
+  PinBuf staging_small;
+  Workspace ws;
   int tuned_leaf[32][8];  // [log2 T][log2 n - 4]
   int tuned_tile[32][8];
   int tuned_stack[32][8];
@@ -103,6 +127,9 @@ struct sdfb_ctx {
   uint64_t device_bytes() const;
 };
 
+int bucket_tris(uint64_t T);
+int bucket_grid(const sdfb_grid_desc &g);
+
 // Reads the tuned leaf / tile / stack table (orchestrate.cu).
 void load_tuning(sdfb_ctx *ctx);
 
@@ -112,10 +139,25 @@ bool grid_ok(const sdfb_grid_desc *g);
 sdfb::GridDev to_dev(const sdfb_grid_desc &g);
 sdfb_opts opts_or_default(const sdfb_opts *o);
 
-// Runs every stage of a bake for `meshes` on stream `st` and waits for it. use_graph: capture the
-// launch sequence into a CUDA graph and replay it while the batch is unchanged.
+// Enqueues every stage of a bake for `meshes` on `st` (nothing waits). Meshes either all carry a
+// resident hierarchy or none does (then one hierarchy over all of them is built). use_graph:
+// capture the launch sequence into a CUDA graph and replay it while the batch is unchanged.
+sdfb_status enqueue_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, std::vector<PlanMesh> &meshes,
+                          const sdfb_opts &opts, bool use_graph, BatchState &state);
+// Waits for the stream, reads the device error word and fills stats. SDFB_ERR_BUSY means the
+// crossing list outgrew its buffer: enqueue the same batch again (the buffer has been resized).
+sdfb_status finish_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, const BatchState &state,
+                         const std::vector<PlanMesh> &meshes, sdfb_stats *stats);
+// enqueue + finish, retrying a crossing-list overflow and a shallow-stack overflow.
 sdfb_status run_batch(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &meshes, const sdfb_opts &opts,
                       bool use_graph, sdfb_stats *stats);
+// Builds the hierarchy of one mesh (and of its caps when cT > 0) into `mem` / `cap_mem`, which
+// must hold resident_bytes(T) / resident_bytes(cT, true). Enqueued on st with ws's temporaries.
+size_t resident_bytes(uint64_t tris, bool with_areas = false);
+sdfb_status build_resident(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, const PlanMesh &mesh, void *mem,
+                           ResidentBvh &out, void *cap_mem, ResidentBvh &cap_out);
 
-// gwn.cu: flips the sign of cells whose generalized winding number says inside.
-sdfb_status gwn_apply(sdfb_ctx *ctx, cudaStream_t st, const GwnInput &in);
+// gwn.cu: flips the sign of cells whose generalized winding number says inside (enqueued only).
+size_t gwn_temp_bytes(uint64_t gwn_cells);
+cudaError_t gwn_enqueue(const GwnInput &in, void *temp, int num_sms, cudaStream_t st);
+uint64_t *gwn_refine_counter(void *temp);

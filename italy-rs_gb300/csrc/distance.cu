@@ -42,10 +42,6 @@ __global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a) {
   const BatchDev &B = a.batch;
   unsigned long long box_tests = 0, tri_tests = 0;
   bool overflow = false, corrupt = false;
-  // A correct tree expands each inner node at most once per tile and pops at most once per
-  // push; anything longer means a corrupt tree, and the walk stops with an error.
-  const long long step_limit = 2ll * a.num_nodes + 64;
-  const int num_tris = static_cast<int>(B.total_tris);
 
   for (;;) {
     unsigned long long tile = 0;
@@ -55,6 +51,12 @@ __global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a) {
     const int mesh = find_mesh(B.tile_starts, B.num_meshes, tile);
     const MeshRec &M = B.recs[mesh];
     const GridDev g = M.g;
+    const Node *__restrict__ nodes = M.nodes;
+    const TriRec *__restrict__ tris = M.tris;
+    const int num_nodes = M.bvh_nodes, num_tris = M.bvh_tris;
+    // A correct tree expands each inner node at most once per tile and pops at most once per
+    // push; anything longer means a corrupt tree, and the walk stops with an error.
+    const long long step_limit = 2ll * num_nodes + 64;
     const unsigned long long local = tile - B.tile_starts[mesh];
     const int tiles_x = (g.nx + TX - 1) / TX, tiles_y = (g.ny + TY - 1) / TY;
     const int tx = static_cast<int>(local % tiles_x);
@@ -79,7 +81,7 @@ __global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a) {
         return;
       }
       for (int k = 0; k < count; ++k) {
-        const TriRec *tr = a.tris + first + k;
+        const TriRec *tr = tris + first + k;
         const float4 r0 = __ldg(&tr->r0), r1 = __ldg(&tr->r1), r2 = __ldg(&tr->r2), r3 = __ldg(&tr->r3);
 #pragma unroll
         for (int v = 0; v < VPL; ++v) best[v] = fminf(best[v], point_tri_dist2(px, py, pz[v], r0, r1, r2, r3));
@@ -89,7 +91,7 @@ __global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a) {
 
     int cur = M.root, sp = 0, stk0 = 0, stk1 = 0;
     for (long long steps = 0;; ++steps) {
-      if (steps > step_limit || cur >= a.num_nodes) {
+      if (steps > step_limit || cur >= num_nodes) {
         corrupt = true;
         break;
       }
@@ -97,11 +99,11 @@ __global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a) {
         if (sp == 0) break;
         --sp;
         const int e = __shfl_sync(kFull, (STACK == 32 || sp < 32) ? stk0 : stk1, sp & 31);
-        if ((e >> 1) >= a.num_nodes) {
+        if ((e >> 1) >= num_nodes) {
           corrupt = true;
           break;
         }
-        const Node *np = a.nodes + (e >> 1);
+        const Node *np = nodes + (e >> 1);
         const float4 n0 = __ldg(&np->n0), n1 = __ldg(&np->n1), n2 = __ldg(&np->n2);
         const int4 n3 = __ldg(&np->n3);
         float lx0, ly0, lz0, hx0, hy0, hz0;
@@ -123,7 +125,7 @@ __global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a) {
         continue;
       }
       const int node = cur;
-      const Node *np = a.nodes + node;
+      const Node *np = nodes + node;
       const float4 n0 = __ldg(&np->n0), n1 = __ldg(&np->n1), n2 = __ldg(&np->n2);
       const int4 n3 = __ldg(&np->n3);
       float d0[VPL], d1[VPL];

@@ -52,17 +52,11 @@ __device__ __forceinline__ T solid_angle(V3<T> a, V3<T> b, V3<T> c) {
 }
 
 struct GwnArgs {
-  BatchDev batch;
+  BatchDev batch;  // each GWN mesh record names its caps hierarchy
   const uint64_t *col_start;
   const float *col_z;
   const int8_t *col_s;
-  const Node *cap_nodes;
-  const TriRec *cap_tris;
-  const float *cap_area;       // per inner node of the caps hierarchy
-  const uint32_t *cap_order;   // local cap triangle of each cap record
-  int cap_num_nodes, cap_num_inner, cap_num_tris;
   float band_voxels;
-  float *dummy;
   uint64_t *refine;
   unsigned long long *refine_count;
   uint64_t *direct;
@@ -95,7 +89,7 @@ __device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, T qx,
                           T &eps, bool &corrupt) {
   const int lane = threadIdx.x & 31;
   int cur = M.cap_root, sp = 0, stk0 = 0, stk1 = 0;
-  const long long step_limit = 2ll * a.cap_num_nodes + 64;
+  const long long step_limit = 2ll * M.cap_nodes_n + 64;
   const float fx = float(qx), fy = float(qy), fz = float(qz);
   auto push = [&](int e) {
     if (sp < kStack) {
@@ -115,11 +109,11 @@ __device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, T qx,
       --sp;
       cur = __shfl_sync(kFull, sp < 32 ? stk0 : stk1, sp & 31);
     }
-    if (steps > step_limit || cur >= a.cap_num_nodes) {
+    if (steps > step_limit || cur >= M.cap_nodes_n) {
       corrupt = true;
       break;
     }
-    const Node *np = a.cap_nodes + cur;
+    const Node *np = M.cap_nodes + cur;
     const float4 n0 = __ldg(&np->n0), n1 = __ldg(&np->n1), n2 = __ldg(&np->n2);
     const int4 n3 = __ldg(&np->n3);
     const int refs[2] = {n3.x, n3.y}, cnts[2] = {n3.z, n3.w};
@@ -130,19 +124,19 @@ __device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, T qx,
       const float d2 = box_d2(fx, fy, fz, n0, n1, n2, k);
       float area;
       if (cnts[k] == 0) {
-        if (refs[k] >= a.cap_num_inner) {
+        if (refs[k] >= M.cap_inner_n) {
           corrupt = true;
           continue;
         }
-        area = __ldg(a.cap_area + refs[k]);
+        area = __ldg(M.cap_area + refs[k]);
       } else {
-        if (refs[k] < 0 || cnts[k] > a.cap_num_tris - refs[k]) {
+        if (refs[k] < 0 || cnts[k] > M.cap_recs_n - refs[k]) {
           corrupt = true;
           continue;
         }
         area = 0.0f;
         for (int j = 0; j < cnts[k]; ++j) {
-          const float4 r3 = __ldg(&a.cap_tris[refs[k] + j].r3);
+          const float4 r3 = __ldg(&M.cap_trec[refs[k] + j].r3);
           area += 0.5f * sqrtf(r3.x * r3.x + r3.y * r3.y + r3.z * r3.z);
         }
       }
@@ -159,7 +153,7 @@ __device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, T qx,
       }
       for (int j = 0; j < cnts[k]; ++j) {
         if (EXACT64) {
-          const uint32_t t = __ldg(a.cap_order + refs[k] + j);
+          const uint32_t t = __ldg(M.cap_order + refs[k] + j);
           V3<T> p[3];
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
@@ -169,7 +163,7 @@ __device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, T qx,
           }
           wex += solid_angle<T>(p[0], p[1], p[2]);
         } else {
-          const TriRec *tr = a.cap_tris + refs[k] + j;
+          const TriRec *tr = M.cap_trec + refs[k] + j;
           const float4 r0 = __ldg(&tr->r0), r1 = __ldg(&tr->r1), r2 = __ldg(&tr->r2);
           const V3<T> p{T(r0.x) - qx, T(r0.y) - qy, T(r0.z) - qz};
           wex += solid_angle<T>(p, {p.x + T(r1.x), p.y + T(r1.y), p.z + T(r1.z)},
@@ -234,8 +228,10 @@ __device__ __forceinline__ void cell_of(const BatchDev &B, uint64_t gcell, int &
   vz = static_cast<int>(cell / (uint64_t(g.nx) * g.ny));
 }
 
-// Pass 2: FP64, one refine cell per lane.
-__global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a, unsigned long long n) {
+// Pass 2: FP64, one refine cell per lane; a persistent grid that reads the list length on the
+// device, so the whole pass needs no host round trip.
+__global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a) {
+  const unsigned long long n = *a.refine_count;
   const int lane = threadIdx.x & 31;
   const BatchDev &B = a.batch;
   bool corrupt = false;
@@ -323,27 +319,19 @@ __global__ __launch_bounds__(kThreads) void k_gwn_direct(GwnArgs a) {
 
 }  // namespace
 
-sdfb_status gwn_apply(sdfb_ctx *ctx, cudaStream_t st, const GwnInput &in) {
+size_t gwn_temp_bytes(uint64_t gwn_cells) { return 256 + 2 * ((gwn_cells * 8 + 255) & ~size_t(255)); }
+
+cudaError_t gwn_enqueue(const GwnInput &in, void *temp, int num_sms, cudaStream_t st) {
   const BatchDev &B = in.batch;
-  if (B.total_gwn_tiles == 0) return SDFB_OK;
-  const uint64_t cells = in.gwn_cells;
-  const size_t list_bytes = ((cells * 8 + 255) & ~size_t(255));
-  if (!ctx->gwn_tmp.ensure(256 + 2 * list_bytes))
-    return ctx_fail(ctx, SDFB_ERR_OUT_OF_MEMORY, "winding-number workspace");
-  char *base = static_cast<char *>(ctx->gwn_tmp.p);
+  if (B.total_gwn_tiles == 0) return cudaSuccess;
+  const size_t list_bytes = (in.gwn_cells * 8 + 255) & ~size_t(255);
+  char *base = static_cast<char *>(temp);
   unsigned long long *counters = reinterpret_cast<unsigned long long *>(base);  // [0] tiles [1] refine [2] direct
   GwnArgs a;
   a.batch = B;
   a.col_start = in.col_start;
   a.col_z = in.col_z;
   a.col_s = in.col_s;
-  a.cap_nodes = in.caps.nodes;
-  a.cap_tris = in.caps.tris;
-  a.cap_area = in.caps.node_area;
-  a.cap_order = in.caps.leaf_order;
-  a.cap_num_nodes = in.caps.num_nodes;
-  a.cap_num_inner = in.caps.num_inner;
-  a.cap_num_tris = static_cast<int>(in.cap_total_tris);
   a.band_voxels = in.band_voxels;
   a.refine = reinterpret_cast<uint64_t *>(base + 256);
   a.refine_count = counters + 1;
@@ -352,28 +340,21 @@ sdfb_status gwn_apply(sdfb_ctx *ctx, cudaStream_t st, const GwnInput &in) {
   a.tile_counter = counters;
   a.err = in.err;
   cudaError_t e = cudaMemsetAsync(counters, 0, 64, st);
-  if (e != cudaSuccess) return ctx_cuda(ctx, e, "memset");
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gwn32, kThreads, 0);
-  long long blocks = static_cast<long long>(ctx->num_sms) * std::max(per_sm, 1);
+  if (e != cudaSuccess) return e;
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gwn32, kThreads, 0);
+    per_sm = std::max(per_sm, 1);
+  }
+  long long blocks = static_cast<long long>(num_sms) * per_sm;
   blocks = std::min<long long>(blocks, static_cast<long long>((B.total_gwn_tiles + 7) / 8));
   k_gwn32<<<static_cast<unsigned>(std::max<long long>(blocks, 1)), kThreads, 0, st>>>(a);
   note_launch();
-  if ((e = cudaGetLastError()) != cudaSuccess) return ctx_cuda(ctx, e, "k_gwn32");
-  // The refine count sizes pass 2: read it back (the bake synchronises at its end anyway).
-  unsigned long long n_refine = 0;
-  if ((e = cudaMemcpyAsync(&n_refine, counters + 1, 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-      (e = cudaStreamSynchronize(st)) != cudaSuccess)
-    return ctx_cuda(ctx, e, "refine count");
-  if (n_refine) {
-    const unsigned long long warps = (n_refine + 31) / 32;
-    const unsigned g2 = static_cast<unsigned>(std::min<unsigned long long>((warps + 7) / 8, 1ull << 20));
-    k_gwn64<<<std::max(g2, 1u), kThreads, 0, st>>>(a, n_refine);
-    note_launch();
-    k_gwn_direct<<<static_cast<unsigned>(ctx->num_sms * 4), kThreads, 0, st>>>(a);
-    note_launch();
-    if ((e = cudaGetLastError()) != cudaSuccess) return ctx_cuda(ctx, e, "k_gwn64");
-  }
-  ctx->gwn_refined = n_refine;
-  return SDFB_OK;
+  k_gwn64<<<static_cast<unsigned>(num_sms * 8), kThreads, 0, st>>>(a);
+  note_launch();
+  k_gwn_direct<<<static_cast<unsigned>(num_sms * 4), kThreads, 0, st>>>(a);
+  note_launch();
+  return cudaGetLastError();
 }
+
+uint64_t *gwn_refine_counter(void *temp) { return reinterpret_cast<uint64_t *>(static_cast<char *>(temp)) + 1; }

@@ -66,7 +66,17 @@ struct MeshRec {
   const float *cverts;    // GWN: vertices of the caps (the parity mesh's vertices + loop centres)
   const uint32_t *cidx;   // GWN: cap triangles
   uint32_t cap_tris;      // GWN: number of cap triangles
-  uint32_t pad;
+  int bvh_nodes;          // node count of the hierarchy holding this mesh (root < bvh_nodes)
+  // The hierarchy holding this mesh: the batch's combined tree, or the mesh's resident tree.
+  const Node *nodes;
+  const TriRec *tris;
+  int bvh_tris;           // records in that hierarchy
+  // GWN: the hierarchy holding this mesh's caps
+  int cap_nodes_n, cap_inner_n, cap_recs_n;
+  const Node *cap_nodes;
+  const TriRec *cap_trec;
+  const float *cap_area;
+  const uint32_t *cap_order;
 };
 
 // Prefix tables of a batch (device): starts[m] of each numbering, starts[M] = total.
@@ -129,10 +139,7 @@ cudaError_t parity_columns(const BatchDev &batch, uint64_t *col_start, float *co
 
 // ---- distance.cu ------------------------------------------------------------------------------
 struct DistanceArgs {
-  BatchDev batch;
-  const Node *nodes;
-  const TriRec *tris;
-  int num_nodes;              // inner nodes + virtual roots
+  BatchDev batch;             // each mesh record names its hierarchy and root
   const uint64_t *col_start;  // parity
   const float *col_z;
   uint32_t *err;

@@ -104,6 +104,41 @@ void build_caps(const float *verts, uint32_t V, const uint32_t *idx, uint32_t T,
 }
 
 // ---------------------------------------------------------------------------------------------
+// Workspace.
+
+bool Workspace::init() {
+  for (auto &e : ev)
+    if (!e && cudaEventCreate(&e) != cudaSuccess) return false;
+  return true;
+}
+
+Workspace::~Workspace() {
+  if (graph) cudaGraphExecDestroy(graph);
+  for (auto &e : ev)
+    if (e) cudaEventDestroy(e);
+}
+
+void Workspace::release() {
+  if (graph) {
+    cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    graph_key.clear();
+  }
+  DevBuf *b[] = {&batch_buf, &bvh, &build_tmp, &par_tmp, &col_start, &col_z, &col_s, &caps_bvh, &caps_tmp, &misc,
+                 &gwn_tmp};
+  for (DevBuf *x : b) x->release();
+  staging.release();
+}
+
+uint64_t Workspace::bytes() const {
+  const DevBuf *b[] = {&batch_buf, &bvh, &build_tmp, &par_tmp, &col_start, &col_z, &col_s, &caps_bvh, &caps_tmp,
+                       &misc, &gwn_tmp};
+  uint64_t s = 0;
+  for (const DevBuf *x : b) s += x->cap;
+  return s;
+}
+
+// ---------------------------------------------------------------------------------------------
 // Batch layout: per-mesh records and prefix tables, uploaded in one copy.
 
 namespace {
@@ -115,6 +150,7 @@ struct Layout {
   std::vector<uint64_t> tri, ptri, tile, gtile, cell, cap_tri, cap_zero;
   uint64_t total_cols = 0, gwn_cells = 0, cap_total = 0;
   int tile_id = 2, stack = 64;
+  bool resident = false;
   size_t o_recs = 0, o_tri = 0, o_ptri = 0, o_tile = 0, o_gtile = 0, o_cell = 0, o_caprecs = 0, o_captri = 0,
          o_capzero = 0, bytes = 0;
 };
@@ -130,6 +166,7 @@ void make_layout(sdfb_ctx *ctx, const std::vector<PlanMesh> &ms, const sdfb_opts
   const int tb = bucket_tris(ms[big].T), nb = bucket_grid(ms[big].grid);
   L.tile_id = (o.tile >= 1 && o.tile <= tile_shape_count()) ? o.tile - 1 : ctx->tuned_tile[tb][nb];
   L.stack = (o.stack_depth == 32 || o.stack_depth == 64) ? o.stack_depth : ctx->tuned_stack[tb][nb];
+  L.resident = ms[0].bvh != nullptr;
   uint64_t T_total = 0;
   for (const auto &p : ms) T_total += p.T;
   const int num_inner = T_total >= 2 ? static_cast<int>(T_total - 1) : 0;
@@ -163,6 +200,13 @@ void make_layout(sdfb_ctx *ctx, const std::vector<PlanMesh> &ms, const sdfb_opts
     r.leaf_size = std::max(1, std::min(leaf, 16));
     r.root = num_inner + m;
     r.cap_root = -1;
+    if (p.bvh) {
+      r.nodes = p.bvh->nodes;
+      r.tris = p.bvh->tris;
+      r.bvh_nodes = p.bvh->num_nodes;
+      r.bvh_tris = p.bvh->num_tris;
+      r.root = p.bvh->root;
+    }
     const uint64_t cells = uint64_t(p.grid.nx) * p.grid.ny * p.grid.nz;
     r.tri_base = L.tri[m];
     r.cell_base = L.cell[m];
@@ -182,7 +226,16 @@ void make_layout(sdfb_ctx *ctx, const std::vector<PlanMesh> &ms, const sdfb_opts
       r.cverts = p.cverts;
       r.cidx = p.cidx;
       r.cap_tris = p.cT;
-      if (p.cT > 0) {
+      if (p.caps) {
+        r.cap_root = p.caps->root;
+        r.cap_nodes = p.caps->nodes;
+        r.cap_trec = p.caps->tris;
+        r.cap_area = p.caps->node_area;
+        r.cap_order = p.caps->leaf_order;
+        r.cap_nodes_n = p.caps->num_nodes;
+        r.cap_inner_n = p.caps->num_inner;
+        r.cap_recs_n = p.caps->num_tris;
+      } else if (p.cT > 0) {
         MeshRec c;
         std::memset(&c, 0, sizeof c);
         c.verts = p.cverts;
@@ -202,7 +255,7 @@ void make_layout(sdfb_ctx *ctx, const std::vector<PlanMesh> &ms, const sdfb_opts
   const int K = static_cast<int>(L.cap_recs.size());
   const int cap_inner = L.cap_total >= 2 ? static_cast<int>(L.cap_total - 1) : 0;
   for (int m = 0; m < M; ++m)
-    if (L.recs[m].cap_root >= 0) L.recs[m].cap_root += cap_inner;
+    if (L.recs[m].cap_root >= 0 && !ms[m].caps) L.recs[m].cap_root += cap_inner;
   for (int k = 0; k < K; ++k) L.cap_recs[k].root = cap_inner + k;
   L.cap_zero.assign(K + 1, 0);
   size_t off = 0;
@@ -221,6 +274,27 @@ void make_layout(sdfb_ctx *ctx, const std::vector<PlanMesh> &ms, const sdfb_opts
   L.o_captri = put((K + 1) * 8);
   L.o_capzero = put((K + 1) * 8);
   L.bytes = off;
+}
+
+// Points the records at the combined hierarchies built for this batch.
+void bind_built(Layout &L, const BvhDev &bvh, const BvhDev *caps) {
+  for (auto &r : L.recs) {
+    if (bvh.nodes) {
+      r.nodes = bvh.nodes;
+      r.tris = bvh.tris;
+      r.bvh_nodes = bvh.num_nodes;
+      r.bvh_tris = static_cast<int>(L.tri.back());
+    }
+    if (caps && r.cap_root >= 0 && !r.cap_nodes) {
+      r.cap_nodes = caps->nodes;
+      r.cap_trec = caps->tris;
+      r.cap_area = caps->node_area;
+      r.cap_order = caps->leaf_order;
+      r.cap_nodes_n = caps->num_nodes;
+      r.cap_inner_n = caps->num_inner;
+      r.cap_recs_n = static_cast<int>(L.cap_total);
+    }
+  }
 }
 
 void fill_staging(const Layout &L, char *s) {
@@ -267,9 +341,14 @@ BatchDev caps_dev(const Layout &L, char *d) {
 
 }  // namespace
 
-sdfb_status run_batch(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &ms, const sdfb_opts &o, bool use_graph,
-                      sdfb_stats *stats) {
+sdfb_status enqueue_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, std::vector<PlanMesh> &ms,
+                          const sdfb_opts &o, bool use_graph, BatchState &S) {
   if (ms.empty()) return ctx_fail(ctx, SDFB_ERR_INVALID_ARGUMENT, "empty batch");
+  cudaGetLastError();  // start from a clean error state
+  if (!ws.init()) return ctx_fail(ctx, SDFB_ERR_CUDA, "cannot create events");
+  for (const auto &p : ms)
+    if ((p.bvh != nullptr) != (ms[0].bvh != nullptr))
+      return ctx_fail(ctx, SDFB_ERR_INTERNAL, "a batch mixes resident and unbuilt meshes");
   Layout L;
   make_layout(ctx, ms, o, L);
   const int M = static_cast<int>(ms.size());
@@ -278,96 +357,113 @@ sdfb_status run_batch(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &ms,
   if (T == 0) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh has no triangles");
   if (T >= (1ull << 31) || L.ptri.back() >= (1ull << 31) || M >= (1 << 25))
     return ctx_fail(ctx, SDFB_ERR_INVALID_ARGUMENT, "batch too large");
-  const bool any_gwn = L.gtile.back() > 0;
-  const bool any_cross = L.ptri.back() > 0;
+  S = BatchState();
+  S.any_gwn = L.gtile.back() > 0;
+  S.any_cross = L.ptri.back() > 0;
+  S.total_cols = L.total_cols;
+  S.total_cells = L.cell.back();
+  S.total_tris = T;
+  S.tile_id = L.tile_id;
+  S.stack = L.stack;
+  S.leaf0 = L.recs[0].leaf_size;
   const bool any_occ = std::any_of(ms.begin(), ms.end(), [](const PlanMesh &p) { return p.occ != nullptr; });
+  const bool build = !L.resident;
 
   // Workspace.
-  ENSURE(ctx->batch_buf, L.bytes);
-  if (!ctx->staging.ensure(L.bytes)) return ctx_fail(ctx, SDFB_ERR_OUT_OF_MEMORY, "pinned staging");
-  ENSURE(ctx->bvh, lbvh_bytes(T, M, false));
-  ENSURE(ctx->build_tmp, std::max(lbvh_temp_bytes(T, M), occupancy_temp_bytes(T)));
-  ENSURE(ctx->misc, 256);
-  uint64_t capacity = 0;
-  if (any_cross) {
-    ENSURE(ctx->par_tmp, parity_temp_bytes(L.ptri.back(), L.total_cols));
-    ENSURE(ctx->col_start, (L.total_cols + 1) * 8);
-    capacity = std::max<uint64_t>(ctx->col_capacity_hint, 4 * L.total_cols + 2 * L.ptri.back());
-    ENSURE(ctx->col_z, capacity * 4);
-    ENSURE(ctx->col_s, capacity);
-    capacity = std::min<uint64_t>(ctx->col_z.cap / 4, ctx->col_s.cap);
+  ENSURE(ws.batch_buf, L.bytes);
+  if (!ws.staging.ensure(L.bytes)) return ctx_fail(ctx, SDFB_ERR_OUT_OF_MEMORY, "pinned staging");
+  if (build) ENSURE(ws.bvh, lbvh_bytes(T, M, false));
+  ENSURE(ws.build_tmp, std::max(build ? lbvh_temp_bytes(T, M) : size_t(0), occupancy_temp_bytes(T)));
+  ENSURE(ws.misc, 256);
+  if (S.any_cross) {
+    ENSURE(ws.par_tmp, parity_temp_bytes(L.ptri.back(), L.total_cols));
+    ENSURE(ws.col_start, (L.total_cols + 1) * 8);
+    const uint64_t want = std::max<uint64_t>(ws.col_capacity_hint, 4 * L.total_cols + 2 * L.ptri.back());
+    ENSURE(ws.col_z, want * 4);
+    ENSURE(ws.col_s, want);
+    S.capacity = std::min<uint64_t>(ws.col_z.cap / 4, ws.col_s.cap);
   }
   if (K > 0) {
-    ENSURE(ctx->caps_bvh, lbvh_bytes(L.cap_total, K, true));
-    ENSURE(ctx->caps_tmp, lbvh_temp_bytes(L.cap_total, K));
+    ENSURE(ws.caps_bvh, lbvh_bytes(L.cap_total, K, true));
+    ENSURE(ws.caps_tmp, lbvh_temp_bytes(L.cap_total, K));
   }
-  fill_staging(L, static_cast<char *>(ctx->staging.p));
-  const BatchDev B = batch_dev(L, static_cast<char *>(ctx->batch_buf.p));
-  BvhDev bvh;
-  lbvh_bind(bvh, ctx->bvh.p, T, M, false);
-  BvhDev caps;
-  BatchDev CB;
-  if (K > 0) {
-    lbvh_bind(caps, ctx->caps_bvh.p, L.cap_total, K, true);
-    CB = caps_dev(L, static_cast<char *>(ctx->batch_buf.p));
-  }
-  uint32_t *d_err = static_cast<uint32_t *>(ctx->misc.p);
-  unsigned long long *d_tile = reinterpret_cast<unsigned long long *>(static_cast<char *>(ctx->misc.p) + 64);
-  unsigned long long *d_work = reinterpret_cast<unsigned long long *>(static_cast<char *>(ctx->misc.p) + 128);
+  if (S.any_gwn) ENSURE(ws.gwn_tmp, gwn_temp_bytes(L.gwn_cells));
+  BvhDev bvh, caps;
+  if (build) lbvh_bind(bvh, ws.bvh.p, T, M, false);
+  if (K > 0) lbvh_bind(caps, ws.caps_bvh.p, L.cap_total, K, true);
+  bind_built(L, build ? bvh : BvhDev(), K > 0 ? &caps : nullptr);
+  fill_staging(L, static_cast<char *>(ws.staging.p));
+  const BatchDev B = batch_dev(L, static_cast<char *>(ws.batch_buf.p));
+  const BatchDev CB = K > 0 ? caps_dev(L, static_cast<char *>(ws.batch_buf.p)) : BatchDev();
+  uint32_t *d_err = static_cast<uint32_t *>(ws.misc.p);
+  unsigned long long *d_tile = reinterpret_cast<unsigned long long *>(static_cast<char *>(ws.misc.p) + 64);
+  unsigned long long *d_work = reinterpret_cast<unsigned long long *>(static_cast<char *>(ws.misc.p) + 128);
   unsigned long long *d_sat = d_work + 2;
   DistanceArgs da{};
   da.batch = B;
-  da.nodes = bvh.nodes;
-  da.tris = bvh.tris;
-  da.num_nodes = bvh.num_nodes;
-  da.col_start = static_cast<const uint64_t *>(ctx->col_start.p);
-  da.col_z = static_cast<const float *>(ctx->col_z.p);
+  da.col_start = static_cast<const uint64_t *>(ws.col_start.p);
+  da.col_z = static_cast<const float *>(ws.col_z.p);
   da.err = d_err;
   da.tile_counter = d_tile;
   da.work_counters = o.count_work ? d_work : nullptr;
+  GwnInput gi;
+  gi.batch = B;
+  gi.col_start = static_cast<const uint64_t *>(ws.col_start.p);
+  gi.col_z = static_cast<const float *>(ws.col_z.p);
+  gi.col_s = static_cast<const int8_t *>(ws.col_s.p);
+  gi.band_voxels = o.band_voxels;
+  gi.err = d_err;
+  gi.gwn_cells = L.gwn_cells;
 
+  bool capturing = false;
+  // Inside a capture, an event record must be an external node to time the replay.
+  auto rec = [&](cudaEvent_t e) {
+    return cudaEventRecordWithFlags(e, st, capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
+  };
   auto enqueue = [&]() -> sdfb_status {
-    CK(cudaMemcpyAsync(ctx->batch_buf.p, ctx->staging.p, L.bytes, cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(ctx->misc.p, 0, 256, st));
-    CK(cudaEventRecord(ctx->ev[0], st));
-    CK(lbvh_build(B, bvh, ctx->build_tmp.p, ctx->build_tmp.cap, d_err, st));
-    CK(cudaEventRecord(ctx->ev[1], st));
-    if (any_occ) CK(occupancy_batch(B, nullptr, ctx->build_tmp.p, ctx->build_tmp.cap, d_sat, ctx->num_sms, st));
-    CK(cudaEventRecord(ctx->ev[2], st));
-    if (any_cross)
-      CK(parity_columns(B, static_cast<uint64_t *>(ctx->col_start.p), static_cast<float *>(ctx->col_z.p),
-                        static_cast<int8_t *>(ctx->col_s.p), capacity, ctx->par_tmp.p, ctx->par_tmp.cap, d_err,
+    CK(cudaMemcpyAsync(ws.batch_buf.p, ws.staging.p, L.bytes, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(ws.misc.p, 0, 256, st));
+    CK(rec(ws.ev[0]));
+    if (build) CK(lbvh_build(B, bvh, ws.build_tmp.p, ws.build_tmp.cap, d_err, st));
+    CK(rec(ws.ev[1]));
+    if (any_occ) CK(occupancy_batch(B, nullptr, ws.build_tmp.p, ws.build_tmp.cap, d_sat, ctx->num_sms, st));
+    CK(rec(ws.ev[2]));
+    if (S.any_cross)
+      CK(parity_columns(B, static_cast<uint64_t *>(ws.col_start.p), static_cast<float *>(ws.col_z.p),
+                        static_cast<int8_t *>(ws.col_s.p), S.capacity, ws.par_tmp.p, ws.par_tmp.cap, d_err,
                         ctx->num_sms, st));
-    if (K > 0) CK(lbvh_build(CB, caps, ctx->caps_tmp.p, ctx->caps_tmp.cap, d_err, st));
-    CK(cudaEventRecord(ctx->ev[3], st));
+    if (K > 0) CK(lbvh_build(CB, caps, ws.caps_tmp.p, ws.caps_tmp.cap, d_err, st));
+    CK(rec(ws.ev[3]));
     CK(distance_launch(da, L.tile_id, L.stack, ctx->num_sms, st));
-    CK(cudaEventRecord(ctx->ev[4], st));
+    CK(rec(ws.ev[4]));
+    if (S.any_gwn) CK(gwn_enqueue(gi, ws.gwn_tmp.p, ctx->num_sms, st));
+    CK(rec(ws.ev[5]));
     return SDFB_OK;
   };
 
   const uint64_t launches0 = launch_count();
-  uint64_t launched = 0;
-  sdfb_status s;
-  bool graphed = false;
-  if (use_graph && !any_gwn && !o.count_work) {
+  if (use_graph && !o.count_work) {
     // Key: the uploaded tables plus every buffer and option the launch sequence bakes in.
-    std::vector<uint8_t> key(static_cast<const uint8_t *>(ctx->staging.p),
-                             static_cast<const uint8_t *>(ctx->staging.p) + L.bytes);
-    const void *ptrs[] = {ctx->batch_buf.p, ctx->bvh.p, ctx->build_tmp.p, ctx->par_tmp.p, ctx->col_start.p,
-                          ctx->col_z.p,     ctx->col_s.p, ctx->misc.p,    ctx->staging.p, static_cast<void *>(st)};
-    const uint64_t extra[] = {uint64_t(L.tile_id), uint64_t(L.stack), capacity, L.bytes, ctx->build_tmp.cap,
-                              ctx->par_tmp.cap};
+    std::vector<uint8_t> key(static_cast<const uint8_t *>(ws.staging.p),
+                             static_cast<const uint8_t *>(ws.staging.p) + L.bytes);
+    const void *ptrs[] = {ws.batch_buf.p, ws.bvh.p,  ws.build_tmp.p, ws.par_tmp.p,  ws.col_start.p,
+                          ws.col_z.p,     ws.col_s.p, ws.misc.p,      ws.staging.p,  ws.caps_bvh.p,
+                          ws.caps_tmp.p,  ws.gwn_tmp.p, static_cast<void *>(st)};
+    const uint64_t extra[] = {uint64_t(L.tile_id), uint64_t(L.stack), S.capacity, L.bytes, ws.build_tmp.cap,
+                              ws.par_tmp.cap, ws.caps_tmp.cap, uint64_t(o.band_voxels * 1e6f)};
     key.insert(key.end(), reinterpret_cast<const uint8_t *>(ptrs), reinterpret_cast<const uint8_t *>(ptrs) + sizeof ptrs);
     key.insert(key.end(), reinterpret_cast<const uint8_t *>(extra),
                reinterpret_cast<const uint8_t *>(extra) + sizeof extra);
-    if (!ctx->graph || key != ctx->graph_key) {
-      if (ctx->graph) {
-        cudaGraphExecDestroy(ctx->graph);
-        ctx->graph = nullptr;
-        ctx->graph_key.clear();
+    if (!ws.graph || key != ws.graph_key) {
+      if (ws.graph) {
+        cudaGraphExecDestroy(ws.graph);
+        ws.graph = nullptr;
+        ws.graph_key.clear();
       }
       CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      s = enqueue();
+      capturing = true;
+      const sdfb_status s = enqueue();
+      capturing = false;
       cudaGraph_t g = nullptr;
       const cudaError_t ce = cudaStreamEndCapture(st, &g);
       if (s != SDFB_OK) {
@@ -375,67 +471,46 @@ sdfb_status run_batch(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &ms,
         return s;
       }
       if (ce != cudaSuccess) return ctx_cuda(ctx, ce, "cudaStreamEndCapture");
-      const cudaError_t ie = cudaGraphInstantiate(&ctx->graph, g, 0);
+      const cudaError_t ie = cudaGraphInstantiate(&ws.graph, g, 0);
       cudaGraphDestroy(g);
       if (ie != cudaSuccess) {
-        ctx->graph = nullptr;
+        ws.graph = nullptr;
         return ctx_cuda(ctx, ie, "cudaGraphInstantiate");
       }
-      ctx->graph_key.swap(key);
-      ctx->graph_launches = launch_count() - launches0;
+      ws.graph_key.swap(key);
+      ws.graph_launches = launch_count() - launches0;
     }
-    CK(cudaGraphLaunch(ctx->graph, st));
-    launched = ctx->graph_launches;
-    graphed = true;
+    CK(cudaGraphLaunch(ws.graph, st));
+    S.launched = ws.graph_launches;
+    S.graphed = true;
   } else {
-    if ((s = enqueue()) != SDFB_OK) return s;
+    const sdfb_status s = enqueue();
+    if (s != SDFB_OK) return s;
+    S.launched = launch_count() - launches0;
   }
-  ctx->gwn_refined = 0;
-  if (any_gwn) {
-    // the winding-number pass reads the crossing lists: make sure they fit first
-    uint32_t h_err0 = 0;
-    CK(cudaMemcpyAsync(&h_err0, d_err, 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    if (!(h_err0 & (kErrCrossingOverflow | kErrBadIndex | kErrNonFinite))) {
-      GwnInput gi;
-      gi.batch = B;
-      gi.col_start = static_cast<const uint64_t *>(ctx->col_start.p);
-      gi.col_z = static_cast<const float *>(ctx->col_z.p);
-      gi.col_s = static_cast<const int8_t *>(ctx->col_s.p);
-      gi.caps = caps;
-      gi.cap_total_tris = L.cap_total;
-      gi.band_voxels = o.band_voxels;
-      gi.err = d_err;
-      gi.gwn_cells = L.gwn_cells;
-      if ((s = gwn_apply(ctx, st, gi)) != SDFB_OK) return s;
-    }
-  }
-  CK(cudaEventRecord(ctx->ev[5], st));
-  if (!graphed) launched = launch_count() - launches0;
+  return SDFB_OK;
+}
 
+sdfb_status finish_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, const BatchState &S,
+                         const std::vector<PlanMesh> &ms, sdfb_stats *stats) {
+  uint32_t *d_err = static_cast<uint32_t *>(ws.misc.p);
+  unsigned long long *d_work = reinterpret_cast<unsigned long long *>(static_cast<char *>(ws.misc.p) + 128);
   uint32_t h_err = 0;
   CK(cudaMemcpyAsync(&h_err, d_err, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (h_err & (kErrBadIndex | kErrNonFinite))
     return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "%s",
                     (h_err & kErrBadIndex) ? "triangle index out of range" : "mesh has a non-finite vertex");
-  if (h_err & kErrStackOverflow) {
-    if (L.stack < 64) {  // the tuned shallow stack was too small for this tree: rerun with 64
-      sdfb_opts o2 = o;
-      o2.stack_depth = 64;
-      return run_batch(ctx, st, ms, o2, use_graph, stats);
-    }
-    return ctx_fail(ctx, SDFB_ERR_OVERFLOW, "BVH traversal stack overflow (depth > 64)");
-  }
-  if (h_err & kErrCorruptTree) return ctx_fail(ctx, SDFB_ERR_INTERNAL, "BVH walk met an invalid reference");
   if (h_err & kErrCrossingOverflow) {
     uint64_t need = 0;
-    CK(cudaMemcpy(&need, static_cast<uint64_t *>(ctx->col_start.p) + L.total_cols, 8, cudaMemcpyDeviceToHost));
-    if (need <= capacity) return ctx_fail(ctx, SDFB_ERR_INTERNAL, "crossing list overflow after resize");
-    ctx->col_capacity_hint = need + need / 4 + 1024;
-    return run_batch(ctx, st, ms, o, use_graph, stats);
+    CK(cudaMemcpy(&need, static_cast<uint64_t *>(ws.col_start.p) + S.total_cols, 8, cudaMemcpyDeviceToHost));
+    if (need <= S.capacity) return ctx_fail(ctx, SDFB_ERR_INTERNAL, "crossing list overflow after resize");
+    ws.col_capacity_hint = need + need / 4 + 1024;
+    return ctx_fail(ctx, SDFB_ERR_BUSY, "crossing list resized; enqueue again");
   }
-
+  if (h_err & kErrStackOverflow)
+    return ctx_fail(ctx, SDFB_ERR_OVERFLOW, "BVH traversal stack overflow (depth > %d)", S.stack);
+  if (h_err & kErrCorruptTree) return ctx_fail(ctx, SDFB_ERR_INTERNAL, "BVH walk met an invalid reference");
   if (stats) {
     sdfb_stats sv;
     std::memset(&sv, 0, sizeof sv);
@@ -443,36 +518,126 @@ sdfb_status run_batch(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &ms,
     sv.sign_mode_used = ms[0].sign == kSignParity ? SDFB_SIGN_PARITY
                                                   : (ms[0].sign == kSignGwn ? SDFB_SIGN_GWN : SDFB_SIGN_NONE);
     sv.watertight = ms[0].watertight;
-    sv.leaf_size_used = L.recs[0].leaf_size;
-    sv.tile_used = L.tile_id + 1;
-    sv.stack_used = L.stack;
+    sv.leaf_size_used = S.leaf0;
+    sv.tile_used = S.tile_id + 1;
+    sv.stack_used = S.stack;
     float ms_b = 0, ms_o = 0, ms_s = 0, ms_d = 0, ms_g = 0, tot = 0;
-    cudaEventElapsedTime(&ms_b, ctx->ev[0], ctx->ev[1]);
-    cudaEventElapsedTime(&ms_o, ctx->ev[1], ctx->ev[2]);
-    cudaEventElapsedTime(&ms_s, ctx->ev[2], ctx->ev[3]);
-    cudaEventElapsedTime(&ms_d, ctx->ev[3], ctx->ev[4]);
-    cudaEventElapsedTime(&ms_g, ctx->ev[4], ctx->ev[5]);
-    cudaEventElapsedTime(&tot, ctx->ev[0], ctx->ev[5]);
+    cudaEventElapsedTime(&ms_b, ws.ev[0], ws.ev[1]);
+    cudaEventElapsedTime(&ms_o, ws.ev[1], ws.ev[2]);
+    cudaEventElapsedTime(&ms_s, ws.ev[2], ws.ev[3]);
+    cudaEventElapsedTime(&ms_d, ws.ev[3], ws.ev[4]);
+    cudaEventElapsedTime(&ms_g, ws.ev[4], ws.ev[5]);
+    cudaEventElapsedTime(&tot, ws.ev[0], ws.ev[5]);
     sv.ms_total = tot;
     sv.ms_build = ms_b;
     sv.ms_occupancy = ms_o;
     sv.ms_sign = ms_s + ms_g;
     sv.ms_distance = ms_d;
-    sv.voxels = L.cell.back();
-    sv.triangles = T;
+    sv.voxels = S.total_cells;
+    sv.triangles = S.total_tris;
     unsigned long long w[3] = {0, 0, 0};
     cudaMemcpy(w, d_work, sizeof w, cudaMemcpyDeviceToHost);
     sv.box_tests = w[0];
     sv.tri_tests = w[1];
     sv.sat_tests = w[2];
     sv.flops_distance = double(w[0]) * kFlopsPointBox + double(w[1]) * kFlopsPointTri;
-    if (any_cross)
-      cudaMemcpy(&sv.crossings, static_cast<uint64_t *>(ctx->col_start.p) + L.total_cols, 8, cudaMemcpyDeviceToHost);
-    sv.kernel_launches = launched;
-    sv.gwn_fp64_cells = ctx->gwn_refined;
-    sv.graph_replayed = graphed ? 1 : 0;
+    if (S.any_cross)
+      cudaMemcpy(&sv.crossings, static_cast<uint64_t *>(ws.col_start.p) + S.total_cols, 8, cudaMemcpyDeviceToHost);
+    if (S.any_gwn) cudaMemcpy(&sv.gwn_fp64_cells, gwn_refine_counter(ws.gwn_tmp.p), 8, cudaMemcpyDeviceToHost);
+    sv.kernel_launches = S.launched;
+    sv.graph_replayed = S.graphed ? 1 : 0;
+    cudaGetLastError();  // a failed statistics read does not fail the bake
     const size_t n = std::min<size_t>(stats->struct_size ? stats->struct_size : sizeof sv, sizeof sv);
     std::memcpy(stats, &sv, n);
   }
+  return SDFB_OK;
+}
+
+sdfb_status run_batch(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &ms, const sdfb_opts &o, bool use_graph,
+                      sdfb_stats *stats) {
+  sdfb_opts oo = o;
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    BatchState S;
+    sdfb_status s = enqueue_batch(ctx, ctx->ws, st, ms, oo, use_graph, S);
+    if (s != SDFB_OK) return s;
+    s = finish_batch(ctx, ctx->ws, st, S, ms, stats);
+    if (s == SDFB_ERR_BUSY) continue;  // crossing list resized
+    if (s == SDFB_ERR_OVERFLOW && S.stack < 64) {
+      oo.stack_depth = 64;  // the tuned shallow stack was too small for this tree
+      continue;
+    }
+    return s;
+  }
+  return ctx_fail(ctx, SDFB_ERR_INTERNAL, "bake did not settle after retries");
+}
+
+// ---------------------------------------------------------------------------------------------
+// Resident hierarchies (serving).
+
+size_t resident_bytes(uint64_t tris, bool with_areas) { return lbvh_bytes(tris, 1, with_areas); }
+
+sdfb_status build_resident(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, const PlanMesh &p, void *mem,
+                           ResidentBvh &out, void *cap_mem, ResidentBvh &cap_out) {
+  if (!ws.init()) return ctx_fail(ctx, SDFB_ERR_CUDA, "cannot create events");
+  const bool with_caps = p.cT > 0 && cap_mem;
+  MeshRec r[2];
+  std::memset(r, 0, sizeof r);
+  r[0].verts = p.verts;
+  r[0].idx = p.idx;
+  r[0].num_verts = p.V;
+  r[0].num_tris = p.T;
+  r[0].leaf_size = std::max(1, std::min(p.leaf > 0 ? p.leaf : ctx->tuned_leaf[bucket_tris(p.T)][bucket_grid(p.grid)], 16));
+  r[1].verts = p.cverts;
+  r[1].idx = p.cidx;
+  r[1].num_verts = p.pV;
+  r[1].num_tris = p.cT;
+  r[1].leaf_size = 4;
+  const uint64_t tables[2][2] = {{0, p.T}, {0, p.cT}};
+  const uint64_t zero[2] = {0, 0};
+  const size_t bytes = 256 * 6;
+  ENSURE(ws.batch_buf, bytes);
+  if (!ws.staging.ensure(bytes)) return ctx_fail(ctx, SDFB_ERR_OUT_OF_MEMORY, "pinned staging");
+  ENSURE(ws.build_tmp, std::max(lbvh_temp_bytes(p.T, 1), with_caps ? lbvh_temp_bytes(p.cT, 1) : size_t(0)));
+  ENSURE(ws.misc, 256);
+  char *hs = static_cast<char *>(ws.staging.p);
+  std::memset(hs, 0, bytes);
+  std::memcpy(hs, &r[0], sizeof(MeshRec));
+  std::memcpy(hs + 256, tables[0], 16);
+  std::memcpy(hs + 512, zero, 16);
+  std::memcpy(hs + 768, &r[1], sizeof(MeshRec));
+  std::memcpy(hs + 1024, tables[1], 16);
+  CK(cudaMemcpyAsync(ws.batch_buf.p, hs, bytes, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(ws.misc.p, 0, 256, st));
+  char *d = static_cast<char *>(ws.batch_buf.p);
+  auto one = [&](int off_rec, int off_tab, uint64_t T, void *m, bool areas, ResidentBvh &o) -> sdfb_status {
+    BatchDev B;
+    B.num_meshes = 1;
+    B.recs = reinterpret_cast<const MeshRec *>(d + off_rec);
+    B.tri_starts = reinterpret_cast<const uint64_t *>(d + off_tab);
+    B.ptri_starts = B.tile_starts = B.gwn_tile_starts = B.cell_starts = reinterpret_cast<const uint64_t *>(d + 512);
+    B.total_tris = T;
+    BvhDev b;
+    lbvh_bind(b, m, T, 1, areas);
+    CK(lbvh_build(B, b, ws.build_tmp.p, ws.build_tmp.cap, static_cast<uint32_t *>(ws.misc.p), st));
+    o.nodes = b.nodes;
+    o.tris = b.tris;
+    o.leaf_order = b.leaf_order;
+    o.node_area = b.node_area;
+    o.num_nodes = b.num_nodes;
+    o.num_inner = b.num_inner;
+    o.num_tris = static_cast<int>(T);
+    o.root = b.num_inner;  // the single virtual root
+    return SDFB_OK;
+  };
+  sdfb_status s = one(0, 256, p.T, mem, false, out);
+  if (s != SDFB_OK) return s;
+  if (with_caps && (s = one(768, 1024, p.cT, cap_mem, true, cap_out)) != SDFB_OK) return s;
+  uint32_t h_err = 0;
+  CK(cudaMemcpyAsync(&h_err, ws.misc.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (h_err & (kErrBadIndex | kErrNonFinite))
+    return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "%s",
+                    (h_err & kErrBadIndex) ? "triangle index out of range" : "mesh has a non-finite vertex");
+  if (h_err) return ctx_fail(ctx, SDFB_ERR_INTERNAL, "hierarchy build failed (%u)", h_err);
   return SDFB_OK;
 }

@@ -1,0 +1,583 @@
+// Serving loop: continuous batching of bake requests over device-resident meshes.
+//
+// The reference bakes one mesh per call, rebuilding its acceleration structure and pipeline every
+// time (src/convert/sdf_baker.cpp:150-305). Here a server keeps meshes and their hierarchies
+// resident and runs requests in waves:
+//
+//   * sdfb_mesh_register uploads a mesh, decides its sign mode (weld + watertight gate), caps it
+//     for the winding number when needed, and builds its hierarchy on a registration stream.
+//     Meshes are keyed by a hash of their contents, so a repeat registration is a cache hit.
+//     Resident bytes count against the HBM budget; unreferenced meshes are evicted least
+//     recently used first when a new one needs room.
+//   * sdfb_submit queues a request; the scheduler thread admits queued requests into the next
+//     wave while a wave slot is free and the budget holds (resident meshes + every in-flight
+//     wave's outputs). A wave is one batched launch sequence (orchestrate.cu) over all its
+//     requests; waves run on separate streams, so a wave admitted while others are on the GPU
+//     overlaps with them. Each cell is computed exactly as in a single bake, so a result is the
+//     same alone and in any mix.
+//   * Outputs go straight to the caller's buffers when they are pinned (cudaMemcpyAsync), else
+//     through the wave's pinned staging buffer and a host copy when the wave retires.
+//   * sdfb_poll waits (bounded) on a condition variable for a request's completion.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "api_internal.h"
+#include "common.cuh"
+#include "host_mesh.h"
+#include "kernels.h"
+
+using namespace sdfb;
+
+namespace {
+
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+uint64_t fnv1a(const void *p, size_t n, uint64_t h) {
+  const uint8_t *b = static_cast<const uint8_t *>(p);
+  for (size_t i = 0; i < n; ++i) {
+    h ^= b[i];
+    h *= 0x100000001b3ull;
+  }
+  return h;
+}
+
+// Stream-ordered device allocation (no device-wide synchronisation when freed).
+struct AsyncBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+struct Resident {
+  uint64_t id = 0;
+  AsyncBuf verts, idx, pverts, pidx, cidx, bvh, caps;
+  ResidentBvh tree, cap_tree;
+  uint32_t V = 0, T = 0, pV = 0, pT = 0, cT = 0;
+  int sign = kSignParity, watertight = -1;
+  uint64_t bytes = 0;
+  uint64_t last_use = 0;
+  int refs = 0;  // in-flight requests
+};
+
+struct Request {
+  uint64_t id = 0, mesh = 0;
+  sdfb_grid_desc grid{};
+  sdfb_opts opts{};
+  float *dist_out = nullptr;
+  uint8_t *occ_out = nullptr;
+  bool dist_pinned = false, occ_pinned = false;
+  double t_submit = 0, t_admit = 0, t_done = 0;
+  int status = -1;  // -1 pending, else sdfb_status
+  uint64_t voxels = 0;
+  int was_resident = 0;
+  bool done = false;
+  void *res = nullptr;  // the Resident mesh, pinned by a reference while the request lives
+};
+
+struct Wave {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  Workspace ws;
+  DevBuf out_dist, out_occ;
+  PinBuf stage_dist, stage_occ;
+  std::vector<Request *> reqs;
+  std::vector<uint64_t> offs;  // cell offset of each request in the wave buffers
+  std::vector<PlanMesh> plan;
+  BatchState state;
+  sdfb_opts opts{};
+  uint64_t bytes = 0;  // budget charge of this wave
+  bool busy = false;
+};
+
+bool is_pinned(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+struct sdfb_server {
+  int device = 0;
+  std::unique_ptr<sdfb_ctx> sched, reg;  // private contexts (streams, workspaces, error text)
+  std::vector<std::unique_ptr<Wave>> waves;
+  std::thread thread;
+  std::mutex mu, reg_mu;
+  std::condition_variable cv_work, cv_done;
+  bool stop = false;
+  std::unordered_map<uint64_t, std::unique_ptr<Resident>> meshes;
+  std::deque<Request *> pending;
+  std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
+  uint64_t next_req = 1, tick = 0;
+  uint64_t budget = 0, resident_bytes_used = 0, inflight_bytes = 0;
+  int max_inflight = 64, inflight = 0;
+  uint64_t wave_cells = 1ull << 25;
+  std::string err;
+  cudaMemPool_t pool = nullptr;
+
+  sdfb_status fail(sdfb_status s, const std::string &m) {
+    std::lock_guard<std::mutex> g(err_mu);
+    err = m;
+    return s;
+  }
+  std::mutex err_mu;
+
+  void run();
+  bool launch_wave(Wave &w);
+  void retire_wave(Wave &w);
+  void free_resident(Resident &r, cudaStream_t st);
+  bool make_room(uint64_t need);
+};
+
+namespace {
+
+std::unique_ptr<sdfb_ctx> make_private_ctx(int device, int num_sms, const sdfb_ctx *tuned) {
+  auto c = std::make_unique<sdfb_ctx>();
+  c->device = device;
+  c->num_sms = num_sms;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+  if (!c->ws.init()) return nullptr;
+  std::memcpy(c->tuned_leaf, tuned->tuned_leaf, sizeof c->tuned_leaf);
+  std::memcpy(c->tuned_tile, tuned->tuned_tile, sizeof c->tuned_tile);
+  std::memcpy(c->tuned_stack, tuned->tuned_stack, sizeof c->tuned_stack);
+  return c;
+}
+
+bool async_alloc(AsyncBuf &b, size_t bytes, cudaStream_t st) {
+  if (bytes == 0) return true;
+  if (cudaMallocAsync(&b.p, bytes, st) != cudaSuccess) {
+    cudaGetLastError();
+    b.p = nullptr;
+    return false;
+  }
+  b.bytes = bytes;
+  return true;
+}
+
+void async_free(AsyncBuf &b, cudaStream_t st) {
+  if (b.p) cudaFreeAsync(b.p, st);
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
+}  // namespace
+
+void sdfb_server::free_resident(Resident &r, cudaStream_t st) {
+  AsyncBuf *bs[] = {&r.verts, &r.idx, &r.pverts, &r.pidx, &r.cidx, &r.bvh, &r.caps};
+  for (AsyncBuf *b : bs) async_free(*b, st);
+}
+
+// Evicts unreferenced meshes, least recently used first, until `need` more bytes fit. mu held.
+bool sdfb_server::make_room(uint64_t need) {
+  while (resident_bytes_used + inflight_bytes + need > budget) {
+    Resident *victim = nullptr;
+    for (auto &kv : meshes)
+      if (kv.second->refs == 0 && (!victim || kv.second->last_use < victim->last_use)) victim = kv.second.get();
+    if (!victim) return false;
+    resident_bytes_used -= victim->bytes;
+    free_resident(*victim, sched->stream);
+    meshes.erase(victim->id);
+  }
+  return true;
+}
+
+void enqueue_readback(Wave &w);
+
+bool sdfb_server::launch_wave(Wave &w) {
+  // runs unlocked: every request holds a reference on its mesh, so r->res cannot go away
+  std::vector<PlanMesh> &plan = w.plan;
+  plan.clear();
+  w.offs.clear();
+  uint64_t cells = 0;
+  for (Request *r : w.reqs) {
+    w.offs.push_back(cells);
+    cells += uint64_t(r->grid.nx) * r->grid.ny * r->grid.nz;
+  }
+  const bool any_dist = std::any_of(w.reqs.begin(), w.reqs.end(), [](Request *r) { return r->dist_out != nullptr; });
+  const bool any_occ = std::any_of(w.reqs.begin(), w.reqs.end(), [](Request *r) { return r->occ_out != nullptr; });
+  if ((any_dist && !w.out_dist.ensure(cells * 4)) || (any_occ && !w.out_occ.ensure(cells))) return false;
+  const bool stage_d = std::any_of(w.reqs.begin(), w.reqs.end(), [](Request *r) { return r->dist_out && !r->dist_pinned; });
+  const bool stage_o = std::any_of(w.reqs.begin(), w.reqs.end(), [](Request *r) { return r->occ_out && !r->occ_pinned; });
+  if ((stage_d && !w.stage_dist.ensure(cells * 4)) || (stage_o && !w.stage_occ.ensure(cells))) return false;
+  for (size_t k = 0; k < w.reqs.size(); ++k) {
+    Request *r = w.reqs[k];
+    Resident *m = static_cast<Resident *>(r->res);
+    PlanMesh p;
+    p.verts = static_cast<const float *>(m->verts.p);
+    p.idx = static_cast<const uint32_t *>(m->idx.p);
+    p.V = m->V;
+    p.T = m->T;
+    const int forced = r->opts.sign_mode;
+    p.sign = forced == SDFB_SIGN_NONE ? kSignNone : m->sign;
+    p.watertight = m->watertight;
+    if (m->sign == kSignGwn) {
+      p.pverts = static_cast<const float *>(m->pverts.p);
+      p.pidx = static_cast<const uint32_t *>(m->pidx.p);
+      p.pV = m->pV;
+      p.pT = m->pT;
+      p.cverts = p.pverts;
+      p.cidx = static_cast<const uint32_t *>(m->cidx.p);
+      p.cT = m->cT;
+      p.caps = m->cT ? &m->cap_tree : nullptr;
+    }
+    p.bvh = &m->tree;
+    p.grid = r->grid;
+    p.dist = r->dist_out ? static_cast<float *>(w.out_dist.p) + w.offs[k] : nullptr;
+    p.occ = r->occ_out ? static_cast<uint8_t *>(w.out_occ.p) + w.offs[k] : nullptr;
+    plan.push_back(p);
+  }
+  w.opts = w.reqs[0]->opts;
+  w.opts.sign_mode = SDFB_SIGN_AUTO;  // per-mesh signs are already resolved in the plan
+  sdfb_status s = enqueue_batch(sched.get(), w.ws, w.stream, plan, w.opts, false, w.state);
+  if (s != SDFB_OK) {
+    for (Request *r : w.reqs) r->status = s;
+    return true;
+  }
+  enqueue_readback(w);
+  cudaEventRecord(w.done, w.stream);
+  return true;
+}
+
+// Copies each request's grids out of the wave buffers: straight into pinned caller buffers,
+// through the wave's pinned staging buffer otherwise (finished by retire_wave on the host).
+void enqueue_readback(Wave &w) {
+  for (size_t k = 0; k < w.reqs.size(); ++k) {
+    Request *r = w.reqs[k];
+    const uint64_t n = uint64_t(r->grid.nx) * r->grid.ny * r->grid.nz;
+    if (r->dist_out) {
+      const float *src = static_cast<const float *>(w.out_dist.p) + w.offs[k];
+      void *dst = r->dist_pinned ? static_cast<void *>(r->dist_out)
+                                 : static_cast<void *>(static_cast<float *>(w.stage_dist.p) + w.offs[k]);
+      cudaMemcpyAsync(dst, src, n * 4, cudaMemcpyDeviceToHost, w.stream);
+    }
+    if (r->occ_out) {
+      const uint8_t *src = static_cast<const uint8_t *>(w.out_occ.p) + w.offs[k];
+      void *dst = r->occ_pinned ? static_cast<void *>(r->occ_out)
+                                : static_cast<void *>(static_cast<uint8_t *>(w.stage_occ.p) + w.offs[k]);
+      cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, w.stream);
+    }
+  }
+}
+
+void sdfb_server::retire_wave(Wave &w) {
+  sdfb_status s = SDFB_OK;
+  bool failed_early = false;
+  for (Request *r : w.reqs)
+    if (r->status >= 0) failed_early = true;
+  if (!failed_early) {
+    s = finish_batch(sched.get(), w.ws, w.stream, w.state, w.plan, nullptr);
+    for (int attempt = 0; attempt < 3 && s == SDFB_ERR_BUSY; ++attempt) {  // crossing list resized: run again
+      s = enqueue_batch(sched.get(), w.ws, w.stream, w.plan, w.opts, false, w.state);
+      if (s == SDFB_OK) {
+        enqueue_readback(w);
+        s = finish_batch(sched.get(), w.ws, w.stream, w.state, w.plan, nullptr);
+      }
+    }
+    if (s == SDFB_OK)
+      for (size_t k = 0; k < w.reqs.size(); ++k) {
+        Request *r = w.reqs[k];
+        const uint64_t n = uint64_t(r->grid.nx) * r->grid.ny * r->grid.nz;
+        if (r->dist_out && !r->dist_pinned)
+          std::memcpy(r->dist_out, static_cast<float *>(w.stage_dist.p) + w.offs[k], n * 4);
+        if (r->occ_out && !r->occ_pinned)
+          std::memcpy(r->occ_out, static_cast<uint8_t *>(w.stage_occ.p) + w.offs[k], n);
+      }
+  }
+  const double t = now_ms();
+  std::lock_guard<std::mutex> g(mu);
+  for (Request *r : w.reqs) {
+    if (r->status < 0) r->status = s;
+    r->t_done = t;
+    r->done = true;
+    static_cast<Resident *>(r->res)->refs--;
+  }
+  inflight -= static_cast<int>(w.reqs.size());
+  inflight_bytes -= w.bytes;
+  w.bytes = 0;
+  w.reqs.clear();
+  w.busy = false;
+  cv_done.notify_all();
+}
+
+void sdfb_server::run() {
+  cudaSetDevice(device);
+  for (;;) {
+    // retire finished waves (their event has completed)
+    for (auto &wp : waves) {
+      Wave &w = *wp;
+      if (w.busy && cudaEventQuery(w.done) == cudaSuccess) retire_wave(w);
+      else cudaGetLastError();
+    }
+    Wave *free_slot = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      if (stop && pending.empty() && inflight == 0) break;
+      for (auto &wp : waves)
+        if (!wp->busy) {
+          free_slot = wp.get();
+          break;
+        }
+      if (free_slot && !pending.empty()) {
+        // admit queued requests in arrival order while the wave and the budget hold
+        uint64_t cells = 0;
+        while (!pending.empty() && inflight < max_inflight) {
+          Request *r = pending.front();
+          const uint64_t n = uint64_t(r->grid.nx) * r->grid.ny * r->grid.nz;
+          const uint64_t bytes = n * ((r->dist_out ? 4 : 0) + (r->occ_out ? 1 : 0)) + n / 4;
+          if (!free_slot->reqs.empty() && (cells + n > wave_cells)) break;
+          if (resident_bytes_used + inflight_bytes + bytes > budget) break;
+          pending.pop_front();
+          r->t_admit = now_ms();
+          free_slot->reqs.push_back(r);
+          free_slot->bytes += bytes;
+          inflight_bytes += bytes;
+          inflight++;
+          cells += n;
+        }
+        if (!free_slot->reqs.empty()) free_slot->busy = true;
+        else free_slot = nullptr;
+      } else {
+        free_slot = nullptr;
+      }
+      if (!free_slot) {
+        const bool any_busy = std::any_of(waves.begin(), waves.end(), [](const std::unique_ptr<Wave> &w) { return w->busy; });
+        if (!any_busy) {
+          cv_work.wait_for(lk, std::chrono::milliseconds(2));
+          continue;
+        }
+      }
+    }
+    if (free_slot) {
+      if (!launch_wave(*free_slot)) {
+        std::lock_guard<std::mutex> g(mu);
+        for (Request *r : free_slot->reqs) r->status = SDFB_ERR_OUT_OF_MEMORY;
+      }
+      continue;
+    }
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+}
+
+extern "C" {
+
+sdfb_status sdfb_server_create(sdfb_ctx *ctx, const sdfb_server_opts *opts, sdfb_server **out) {
+  if (!ctx || !out) return SDFB_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  cudaSetDevice(ctx->device);
+  auto srv = std::make_unique<sdfb_server>();
+  srv->device = ctx->device;
+  sdfb_server_opts o;
+  std::memset(&o, 0, sizeof o);
+  if (opts) std::memcpy(&o, opts, std::min<size_t>(sizeof o, opts->struct_size ? opts->struct_size : sizeof o));
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  srv->budget = o.hbm_budget_bytes ? o.hbm_budget_bytes : uint64_t(free_b) * 3 / 4;
+  srv->max_inflight = o.max_inflight > 0 ? o.max_inflight : 64;
+  srv->wave_cells = 1ull << (o.wave_voxels_log2 > 10 && o.wave_voxels_log2 < 36 ? o.wave_voxels_log2 : 25);
+  srv->sched = make_private_ctx(ctx->device, ctx->num_sms, ctx);
+  srv->reg = make_private_ctx(ctx->device, ctx->num_sms, ctx);
+  if (!srv->sched || !srv->reg) return SDFB_ERR_CUDA;
+  // keep freed device memory in the stream-ordered pool for reuse
+  if (cudaDeviceGetDefaultMemPool(&srv->pool, ctx->device) == cudaSuccess) {
+    uint64_t keep = ~0ull;
+    cudaMemPoolSetAttribute(srv->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  const int slots = 3;
+  for (int i = 0; i < slots; ++i) {
+    auto w = std::make_unique<Wave>();
+    if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&w->done, cudaEventDisableTiming) != cudaSuccess || !w->ws.init())
+      return SDFB_ERR_CUDA;
+    srv->waves.push_back(std::move(w));
+  }
+  sdfb_server *raw = srv.release();
+  raw->thread = std::thread([raw] { raw->run(); });
+  *out = raw;
+  return SDFB_OK;
+}
+
+void sdfb_server_destroy(sdfb_server *srv) {
+  if (!srv) return;
+  {
+    std::lock_guard<std::mutex> g(srv->mu);
+    srv->stop = true;
+  }
+  srv->cv_work.notify_all();
+  if (srv->thread.joinable()) srv->thread.join();
+  cudaSetDevice(srv->device);
+  for (auto &kv : srv->meshes) srv->free_resident(*kv.second, srv->sched->stream);
+  cudaStreamSynchronize(srv->sched->stream);
+  for (auto &w : srv->waves) {
+    cudaStreamSynchronize(w->stream);
+    if (w->done) cudaEventDestroy(w->done);
+    if (w->stream) cudaStreamDestroy(w->stream);
+  }
+  delete srv;
+}
+
+const char *sdfb_server_last_error(const sdfb_server *srv) { return srv ? srv->err.c_str() : "null server"; }
+
+sdfb_status sdfb_mesh_register(sdfb_server *srv, const float *verts, uint32_t num_verts, const uint32_t *idx,
+                               uint32_t num_tris, uint64_t *mesh_id) {
+  if (!srv || !verts || !idx || !mesh_id) return SDFB_ERR_INVALID_ARGUMENT;
+  if (num_tris == 0 || num_verts == 0) return srv->fail(SDFB_ERR_BAD_MESH, "mesh has no triangles");
+  for (size_t k = 0; k < size_t(num_tris) * 3; ++k)
+    if (idx[k] >= num_verts) return srv->fail(SDFB_ERR_BAD_MESH, "triangle index out of range");
+  uint64_t h = fnv1a(verts, size_t(num_verts) * 12, 0xcbf29ce484222325ull);
+  h = fnv1a(idx, size_t(num_tris) * 12, h);
+  h = fnv1a(&num_verts, 4, h);
+  *mesh_id = h;
+  {
+    std::lock_guard<std::mutex> g(srv->mu);
+    auto it = srv->meshes.find(h);
+    if (it != srv->meshes.end()) {
+      it->second->last_use = ++srv->tick;
+      return SDFB_OK;
+    }
+  }
+  std::lock_guard<std::mutex> rg(srv->reg_mu);  // one registration at a time
+  cudaSetDevice(srv->device);
+  auto r = std::make_unique<Resident>();
+  r->id = h;
+  r->V = num_verts;
+  r->T = num_tris;
+  const int w = indexed_mesh_watertight(verts, num_verts, idx, num_tris);
+  r->watertight = w == 1 ? 1 : 0;
+  r->sign = w == 1 ? kSignParity : kSignGwn;
+  CapBuild caps;
+  if (r->sign == kSignGwn) {
+    build_caps(verts, num_verts, idx, num_tris, caps);
+    r->pV = static_cast<uint32_t>(caps.verts.size() / 3);
+    r->pT = static_cast<uint32_t>(caps.pidx.size() / 3);
+    r->cT = static_cast<uint32_t>(caps.cidx.size() / 3);
+  }
+  const size_t bvh_bytes = resident_bytes(num_tris, false);
+  const size_t cap_bytes = r->cT ? resident_bytes(r->cT, true) : 0;
+  r->bytes = size_t(num_verts) * 12 + size_t(num_tris) * 12 + bvh_bytes + cap_bytes +
+             (r->sign == kSignGwn ? caps.verts.size() * 4 + caps.pidx.size() * 4 + caps.cidx.size() * 4 : 0);
+  {
+    std::lock_guard<std::mutex> g(srv->mu);
+    if (!srv->make_room(r->bytes))
+      return srv->fail(SDFB_ERR_OUT_OF_MEMORY, "mesh does not fit the HBM budget next to in-flight work");
+    srv->resident_bytes_used += r->bytes;  // reserved now, released on failure
+  }
+  cudaStream_t st = srv->reg->stream;
+  auto undo = [&](sdfb_status s, const std::string &m) {
+    srv->free_resident(*r, st);
+    cudaStreamSynchronize(st);
+    std::lock_guard<std::mutex> g(srv->mu);
+    srv->resident_bytes_used -= r->bytes;
+    return srv->fail(s, m);
+  };
+  if (!async_alloc(r->verts, size_t(num_verts) * 12, st) || !async_alloc(r->idx, size_t(num_tris) * 12, st) ||
+      !async_alloc(r->bvh, bvh_bytes, st))
+    return undo(SDFB_ERR_OUT_OF_MEMORY, "device allocation failed");
+  cudaMemcpyAsync(r->verts.p, verts, size_t(num_verts) * 12, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(r->idx.p, idx, size_t(num_tris) * 12, cudaMemcpyHostToDevice, st);
+  if (r->sign == kSignGwn) {
+    if (!async_alloc(r->pverts, caps.verts.size() * 4, st) || !async_alloc(r->pidx, caps.pidx.size() * 4, st) ||
+        !async_alloc(r->cidx, std::max<size_t>(caps.cidx.size(), 1) * 4, st) ||
+        (cap_bytes && !async_alloc(r->caps, cap_bytes, st)))
+      return undo(SDFB_ERR_OUT_OF_MEMORY, "device allocation failed");
+    cudaMemcpyAsync(r->pverts.p, caps.verts.data(), caps.verts.size() * 4, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(r->pidx.p, caps.pidx.data(), caps.pidx.size() * 4, cudaMemcpyHostToDevice, st);
+    if (!caps.cidx.empty())
+      cudaMemcpyAsync(r->cidx.p, caps.cidx.data(), caps.cidx.size() * 4, cudaMemcpyHostToDevice, st);
+  }
+  PlanMesh p;
+  p.verts = static_cast<const float *>(r->verts.p);
+  p.idx = static_cast<const uint32_t *>(r->idx.p);
+  p.V = num_verts;
+  p.T = num_tris;
+  p.cverts = static_cast<const float *>(r->pverts.p);
+  p.cidx = static_cast<const uint32_t *>(r->cidx.p);
+  p.pV = r->pV;
+  p.cT = r->cT;
+  p.grid.nx = p.grid.ny = p.grid.nz = 256;  // leaf size is tuned for a typical grid
+  const sdfb_status s = build_resident(srv->reg.get(), srv->reg->ws, st, p, r->bvh.p, r->tree, r->caps.p, r->cap_tree);
+  if (s != SDFB_OK) return undo(s, srv->reg->err);
+  std::lock_guard<std::mutex> g(srv->mu);
+  r->last_use = ++srv->tick;
+  srv->meshes[h] = std::move(r);
+  return SDFB_OK;
+}
+
+sdfb_status sdfb_submit(sdfb_server *srv, uint64_t mesh_id, const sdfb_grid_desc *grid, const sdfb_opts *opts,
+                        float *dist_out, uint8_t *occ_out, uint64_t *request_id) {
+  if (!srv || !request_id || !grid_ok(grid)) return SDFB_ERR_INVALID_ARGUMENT;
+  if (!dist_out && !occ_out) return srv->fail(SDFB_ERR_INVALID_ARGUMENT, "no output requested");
+  auto r = std::make_unique<Request>();
+  r->mesh = mesh_id;
+  r->grid = *grid;
+  r->opts = opts_or_default(opts);
+  r->dist_out = r->opts.no_distance ? nullptr : dist_out;
+  r->occ_out = r->opts.no_occupancy ? nullptr : occ_out;
+  r->dist_pinned = is_pinned(r->dist_out);
+  r->occ_pinned = is_pinned(r->occ_out);
+  r->t_submit = now_ms();
+  r->voxels = uint64_t(grid->nx) * grid->ny * grid->nz;
+  {
+    std::lock_guard<std::mutex> g(srv->mu);
+    auto it = srv->meshes.find(mesh_id);
+    if (it == srv->meshes.end()) return srv->fail(SDFB_ERR_NOT_FOUND, "mesh is not registered (or was evicted)");
+    it->second->refs++;
+    it->second->last_use = ++srv->tick;
+    r->res = it->second.get();
+    r->was_resident = 1;
+    r->id = srv->next_req++;
+    *request_id = r->id;
+    srv->pending.push_back(r.get());
+    srv->reqs[r->id] = std::move(r);
+  }
+  srv->cv_work.notify_one();
+  return SDFB_OK;
+}
+
+sdfb_status sdfb_poll(sdfb_server *srv, uint64_t request_id, int32_t timeout_ms, int32_t *done,
+                      sdfb_request_info *info) {
+  if (!srv || !done) return SDFB_ERR_INVALID_ARGUMENT;
+  *done = 0;
+  std::unique_lock<std::mutex> lk(srv->mu);
+  auto it = srv->reqs.find(request_id);
+  if (it == srv->reqs.end()) return SDFB_ERR_NOT_FOUND;
+  Request *r = it->second.get();
+  if (!r->done) {
+    if (timeout_ms < 0) {
+      srv->cv_done.wait(lk, [&] { return r->done; });
+    } else if (timeout_ms > 0) {
+      srv->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return r->done; });
+    }
+  }
+  if (!r->done) return SDFB_OK;
+  *done = 1;
+  if (info) {
+    sdfb_request_info x;
+    std::memset(&x, 0, sizeof x);
+    x.struct_size = sizeof x;
+    x.status = r->status;
+    x.t_submit_ms = r->t_submit;
+    x.t_admit_ms = r->t_admit;
+    x.t_done_ms = r->t_done;
+    x.voxels = r->voxels;
+    x.mesh_was_resident = r->was_resident;
+    std::memcpy(info, &x, std::min<size_t>(info->struct_size ? info->struct_size : sizeof x, sizeof x));
+  }
+  const sdfb_status st = static_cast<sdfb_status>(r->status);
+  srv->reqs.erase(it);
+  return st == SDFB_OK ? SDFB_OK : st;
+}
+
+}  // extern "C"

@@ -122,9 +122,14 @@ cudaError_t sparse_count(const uint8_t *occ, size_t cells, void *temp, size_t te
 // into cells_out (device, total uint32). tri_bits = bits needed for a triangle index.
 cudaError_t sparse_emit(const uint8_t *occ, const uint32_t *first_tri, size_t cells, uint64_t total, int tri_bits,
                         void *temp, size_t temp_bytes, uint32_t *cells_out, cudaStream_t st) {
-  SparseTemp o;  // counts/starts sit at the same offsets as in sparse_count's layout
+  SparseTemp o;
   if (sparse_layout(cells, total, static_cast<char *>(temp), &o) > temp_bytes) return cudaErrorMemoryAllocation;
   const size_t tiles = (cells + kTile - 1) / kTile;
+  // recount: the workspace may have been reallocated since sparse_count
+  k_tile_count<<<static_cast<unsigned>(tiles), kThreads, 0, st>>>(occ, cells, o.counts);
+  note_launch();
+  cudaError_t e0 = exclusive_scan_u32(o.counts, o.starts, tiles, Scratch{o.scratch, o.scratch_bytes}, st);
+  if (e0 != cudaSuccess) return e0;
   k_tile_write<<<static_cast<unsigned>(tiles), kThreads, 0, st>>>(occ, first_tri, cells, o.starts, o.keys, cells_out);
   note_launch();
   cudaError_t e = cudaGetLastError();

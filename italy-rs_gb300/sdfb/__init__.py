@@ -345,3 +345,69 @@ class Context:
 
     def device_bytes(self) -> int:
         return int(self.lib.sdfb_ctx_device_bytes(self.h))
+
+
+class Server:
+    """Continuous-batching bake server over device-resident meshes (sdfb_server_*)."""
+
+    def __init__(self, ctx: Context, hbm_budget_bytes: int = 0, max_inflight: int = 0, wave_voxels_log2: int = 0):
+        self.lib = ctx.lib
+        o = ServerOpts()
+        o.struct_size = C.sizeof(ServerOpts)
+        o.hbm_budget_bytes = int(hbm_budget_bytes)
+        o.max_inflight = int(max_inflight)
+        o.wave_voxels_log2 = int(wave_voxels_log2)
+        h = C.c_void_p()
+        st = self.lib.sdfb_server_create(ctx.h, C.byref(o), C.byref(h))
+        if st != OK:
+            raise SdfbError(st, ctx.error())
+        self.h = h
+        self._keep = {}
+
+    def close(self):
+        if self.h:
+            self.lib.sdfb_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def error(self) -> str:
+        return (self.lib.sdfb_server_last_error(self.h) or b"").decode()
+
+    def register(self, verts, idx) -> int:
+        v = _f32(verts).reshape(-1, 3)
+        i = _u32a(idx).reshape(-1, 3)
+        mid = C.c_uint64()
+        st = self.lib.sdfb_mesh_register(self.h, _ptr(v), len(v), _ptr(i), len(i), C.byref(mid))
+        if st != OK:
+            raise SdfbError(st, self.error())
+        return int(mid.value)
+
+    def submit(self, mesh_id: int, grid: GridDesc, dist: np.ndarray | None, occ: np.ndarray | None,
+               opts: Opts | None = None) -> int:
+        """Queues a bake; dist / occ are caller-owned arrays of grid.cells elements that must stay
+        alive until poll reports the request done."""
+        rid = C.c_uint64()
+        st = self.lib.sdfb_submit(self.h, C.c_uint64(mesh_id), C.byref(grid), C.byref(opts) if opts else None,
+                                  _ptr(dist), _ptr(occ), C.byref(rid))
+        if st != OK:
+            raise SdfbError(st, self.error())
+        self._keep[int(rid.value)] = (dist, occ)
+        return int(rid.value)
+
+    def poll(self, request_id: int, timeout_ms: int = -1):
+        """Returns (done, info dict); raises if the finished request failed."""
+        done = C.c_int32()
+        info = RequestInfo()
+        info.struct_size = C.sizeof(RequestInfo)
+        st = self.lib.sdfb_poll(self.h, C.c_uint64(request_id), int(timeout_ms), C.byref(done), C.byref(info))
+        if done.value:
+            self._keep.pop(request_id, None)
+        if st != OK:
+            raise SdfbError(st, self.error())
+        d = {k: getattr(info, k) for k, _ in RequestInfo._fields_ if k not in ("struct_size", "pad")}
+        return bool(done.value), d

@@ -1,0 +1,89 @@
+"""Serving loop: continuous batching over resident meshes. Every served result must equal the
+same bake run alone through the plain entry point (bit for bit: each cell is computed the same
+way whatever else shares the wave)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_served_equals_plain_in_the_mix(ctx):
+    import sdfb
+    from sdfb import meshgen as mg
+    meshes = [mg.displaced_icosphere(3, 0.3, 1), mg.displaced_torus(40, 12, 0.27, 0.1, 2),
+              mg.displaced_icosphere(4, 0.33, 3)]
+    sizes = [24, 40, 56, 32, 48, 64, 24, 40, 72, 16]
+    with sdfb.Server(ctx, max_inflight=6, wave_voxels_log2=17) as srv:
+        ids = [srv.register(v, f) for v, f in meshes]
+        assert srv.register(*meshes[1]) == ids[1]  # identical contents: the resident copy
+        reqs = []
+        for k, n in enumerate(sizes):
+            g = sdfb.make_grid((-0.5,) * 3, 1.0 / n, (n, n + 1, n - 1))
+            d = np.empty(g.shape, np.float32)
+            o = np.empty(g.shape, np.uint8)
+            reqs.append((srv.submit(ids[k % 3], g, d, o), k % 3, g, d, o))
+        infos = []
+        for rid, m, g, d, o in reqs:
+            done, info = srv.poll(rid, 60000)
+            assert done and info["status"] == 0
+            infos.append(info)
+            d1, o1 = ctx.bake(*meshes[m], g, sdfb.make_opts())
+            assert np.array_equal(o, o1)
+            assert np.array_equal(d, d1)
+        assert all(i["t_submit_ms"] <= i["t_admit_ms"] <= i["t_done_ms"] for i in infos)
+
+
+def test_served_gwn_mesh(ctx):
+    import sdfb
+    from sdfb import meshgen as mg
+    v, f = mg.delete_faces(*mg.displaced_icosphere(3, 0.3, 8), 0.05, 9)
+    g = sdfb.make_grid((-0.5,) * 3, 1.0 / 36, (36, 36, 36))
+    with sdfb.Server(ctx) as srv:
+        mid = srv.register(v, f)
+        d = np.empty(g.shape, np.float32)
+        o = np.empty(g.shape, np.uint8)
+        rid = srv.submit(mid, g, d, o)
+        done, info = srv.poll(rid, 60000)
+        assert done
+    d1, o1 = ctx.bake(v, f, g, sdfb.make_opts())
+    assert np.array_equal(o, o1) and np.array_equal(d, d1)
+
+
+def test_budget_evicts_least_recently_used(ctx):
+    import sdfb
+    from sdfb import meshgen as mg
+    ms = [mg.displaced_icosphere(4, 0.3, s) for s in range(3)]  # 5,120 triangles each
+    per_mesh = 5120 * 160
+    with sdfb.Server(ctx, hbm_budget_bytes=int(per_mesh * 2.5)) as srv:
+        a = srv.register(*ms[0])
+        b = srv.register(*ms[1])
+        srv.register(*ms[0])  # touch a: b is now the least recently used
+        c = srv.register(*ms[2])  # evicts b
+        g = sdfb.make_grid((-0.5,) * 3, 1.0 / 8, (8, 8, 8))
+        d = np.empty(g.shape, np.float32)
+        with pytest.raises(sdfb.SdfbError) as e:
+            srv.submit(b, g, d, None)
+        assert e.value.status == sdfb.ERR_NOT_FOUND
+        for mid in (a, c):
+            rid = srv.submit(mid, g, d, None)
+            assert srv.poll(rid, 60000)[0]
+        with pytest.raises(sdfb.SdfbError) as e:
+            srv.register(*mg.displaced_icosphere(6, 0.3, 4))  # larger than the whole budget
+        assert e.value.status == sdfb.ERR_OUT_OF_MEMORY
+
+
+def test_pinned_outputs(ctx):
+    torch = pytest.importorskip("torch")
+    import sdfb
+    from sdfb import meshgen as mg
+    v, f = mg.displaced_torus(30, 10, 0.27, 0.1, 5)
+    g = sdfb.make_grid((-0.5,) * 3, 1.0 / 40, (40, 40, 40))
+    d = torch.empty(g.cells, dtype=torch.float32).pin_memory().numpy().reshape(g.shape)
+    o = torch.empty(g.cells, dtype=torch.uint8).pin_memory().numpy().reshape(g.shape)
+    with sdfb.Server(ctx) as srv:
+        rid = srv.submit(srv.register(v, f), g, d, o)
+        assert srv.poll(rid, 60000)[0]
+    d1, o1 = ctx.bake(v, f, g, sdfb.make_opts())
+    assert np.array_equal(d, d1) and np.array_equal(o, o1)
