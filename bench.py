@@ -1,32 +1,42 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 mesh -> SDF bake.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload batch64|displaced-sphere-256] [--serve-seconds S] [--no-serve]
 
-Workload (default ``displaced-sphere-256``): the level-6 displaced icosphere (81,920 triangles,
-radius 0.35, 8 seeded sinusoids of total amplitude 0.05) baked onto a 256^3 FP32 grid over
-[-0.5, 0.5]^3 with occupancy and exact parity sign. One step = one full bake (BVH build,
-occupancy, parity crossings, distance + sign) of that mesh. Seeded synthetic input.
+Workloads (seeded synthetic meshes generated in-process; no dataset is involved):
 
-``value``  voxels/s with the mesh already in HBM (sdfb_bake_device), CUDA events on the bake's
-           stream, L2 flushed (512 MB write) before every timed step.
-``e2e``    the same metric through sdfb_bake with pinned host buffers: mesh upload, bake and the
-           read-back of the distance and occupancy grids inside the timed region.
-``roofline`` FP32 (the distance kernel is CUDA-core FMA work, no contraction): algorithmic flops
-           per launch from the counting build of the same kernel / the kernel's mean CUDA-event
-           time in the timed steps, against an SGEMM (cuBLAS, FP32, no TF32) measured in this run.
-``cpu_baseline`` the CPU bake of the same mesh and grid on this host: occupancy by the reference's
-           own SAT code where it was compiled (oracle/_ref) else by the oracle's restatement, FP64
-           distance and exact parity sign from the oracle, all host threads.
+* ``batch64`` (default): 64 meshes, triangle counts log-uniform in [1e3, 1e6] (displaced icospheres
+  and tori), grids drawn uniformly from {32, 64, 128, 256}^3 over [-0.5, 0.5]^3, exact parity sign,
+  occupancy on. One step = the whole batch baked by one call (sdfb_bake_batch_device: one BVH
+  build, one persistent distance launch over every mesh's tiles, replayed from a CUDA graph).
+  ``value`` is voxels/s of that step with meshes and outputs in HBM; ``plain`` times the same 64
+  meshes through 64 single-mesh calls (sdfb_bake_device) in the same run.
+* ``displaced-sphere-256``: the level-6 displaced icosphere (81,920 triangles) on a 256^3 grid, one
+  single-mesh bake per step.
 
-Multi-GPU (torchrun): every rank bakes its own copy (replicas; the bake has no exchange step);
-``value`` sums all ranks' voxels over the slowest rank's time.
+Also reported: ``served`` -- a Poisson stream (200 requests/s for --serve-seconds, default 60) of
+meshes drawn as in batch64 (30% of requests repeat an earlier mesh, the rest bring a new one) fed
+to the serving loop under a 150 GB budget, with voxels/s and p50/p99 latency (arrival to
+completion), beside the same stream's first seconds served by plain per-request bakes;
+``single_mesh`` -- the 256^3 displaced-sphere bake; ``roofline`` of the distance kernel (FP32
+CUDA-core work: algorithmic flops per launch from the counting build of the same kernel over the
+kernel's CUDA-event time, against a cuBLAS SGEMM measured in this run); ``cpu_baseline`` -- the
+CPU bake (the reference's own SAT occupancy where it was compiled, else the oracle's restatement;
+FP64 distance and exact parity from the oracle on all host threads) on a bounded sample.
+
+Timing: W >= 3 untimed warm-up steps; CUDA events on the bake's stream; a 512 MB L2 flush
+before every timed step; nvidia-smi clocks sampled during the timed region. Multi-GPU
+(torchrun): every rank bakes its own replica (the bake has no exchange step); ``value`` sums all
+ranks' voxels over the slowest rank's time.
 """
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
+import queue
 import statistics
 import subprocess
 import sys
@@ -43,44 +53,47 @@ METRIC = "SDF bake voxels/s & p99 latency, served vs plain, 1 GB300, err<=1e-5*d
 L2_FLUSH_BYTES = 512 << 20
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="displaced-sphere-256")
+    ap.add_argument("--workload", default="batch64", choices=["batch64", "displaced-sphere-256"])
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def aggregate(voxels_per_rank: float, seconds_per_rank: float, all_reduce_max=None, all_reduce_sum=None):
+    """Whole-job throughput: the sum of every rank's voxels over the slowest rank's time."""
+    secs = all_reduce_max(seconds_per_rank) if all_reduce_max else seconds_per_rank
+    vox = all_reduce_sum(voxels_per_rank) if all_reduce_sum else voxels_per_rank
+    return vox / secs, secs
 
 
 # ---------------------------------------------------------------------------------------------
 # Workloads
 
 
-def workload(name: str):
+def batch64_meshes():
     from sdfb import meshgen as mg
-    if name == "displaced-sphere-256":
-        v, i = mg.displaced_sphere_mesh(seed=1234)
-        origin, voxel, n = mg.unit_grid(256)
-        cfg = {"workload": name, "mesh": "icosphere L6 displaced (8 sinusoids, amp 0.05), r=0.35",
-               "triangles": int(len(i)), "grid": list(n), "bounds": [[-0.5] * 3, [0.5] * 3], "sign": "parity",
-               "seed": 1234}
-        return v, i, origin, voxel, n, cfg
-    if name == "uv-sphere-64":
-        v, i = mg.uv_sphere_mesh(0.4, 64, 32)
-        origin, voxel, n = mg.unit_grid(64)
-        cfg = {"workload": name, "mesh": "UV sphere r=0.4, 64 lon x 32 lat", "triangles": int(len(i)),
-               "grid": list(n), "bounds": [[-0.5] * 3, [0.5] * 3], "sign": "parity"}
-        return v, i, origin, voxel, n, cfg
-    raise SystemExit(f"unknown workload {name}")
+    return mg.batch_meshes(64, seed=2024)
+
+
+def sphere256():
+    from sdfb import meshgen as mg
+    v, i = mg.displaced_sphere_mesh(seed=1234)
+    return v, i, 256
+
+
+def unit_grid(sdfb, n):
+    return sdfb.make_grid((-0.5, -0.5, -0.5), 1.0 / n, (n, n, n))
 
 
 # ---------------------------------------------------------------------------------------------
@@ -88,7 +101,7 @@ def workload(name: str):
 
 
 class ClockSampler:
-    """nvidia-smi samples every 200 ms while the timed region runs."""
+    """nvidia-smi samples every 200 ms while a timed region runs."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -125,7 +138,7 @@ class ClockSampler:
             self.proc.kill()
         if self.t:
             self.t.join(timeout=2)
-        sm, smax, reasons = [], [], set()
+        sm, smax, pw, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
@@ -134,25 +147,40 @@ class ClockSampler:
             try:
                 sm.append(float(parts[1]))
                 smax.append(float(parts[2]))
+                pw.append(float(parts[3]))
             except ValueError:
                 continue
             for nm, val in zip(names, parts[5:9]):
                 if val.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(pw) if pw else None}
 
 
 # ---------------------------------------------------------------------------------------------
 # CPU baseline (the reference's CPU occupancy code + the FP64 oracle)
 
 
-def cpu_bake(v, i, origin, voxel, n, threads=0):
-    """One CPU bake of the workload; returns (seconds, kind)."""
-    from oracle.oracle import Oracle, soup_of
+def cpu_bake(orc, ref, v, i, n):
+    """One CPU bake of mesh (v, i) on the n^3 unit grid; returns seconds."""
+    from oracle.oracle import soup_of
+    origin, voxel, dims = (-0.5, -0.5, -0.5), 1.0 / n, (n, n, n)
+    soup = soup_of(v, i) if ref is not None else None
+    t0 = time.perf_counter()
+    if ref is not None:
+        ref.occupancy(soup, origin, voxel, dims)
+    else:
+        orc.occupancy(v, i, origin, voxel, dims)
+    d = orc.distance(v, i, origin, voxel, dims)
+    s = orc.sign_parity(v, i, origin, voxel, dims, axis=2)
+    (d * s).astype("float32")
+    return time.perf_counter() - t0
+
+
+def cpu_tools():
+    from oracle.oracle import Oracle
     orc = Oracle()
-    kind = "port"
-    ref = None
+    ref, kind = None, "port"
     try:
         from oracle import build_oracle
         if os.path.exists(build_oracle.REF_SO):
@@ -161,62 +189,59 @@ def cpu_bake(v, i, origin, voxel, n, threads=0):
             kind = "reference"
     except Exception:
         ref = None
-    soup = soup_of(v, i) if ref is not None else None
-    t0 = time.perf_counter()
-    if ref is not None:
-        occ = ref.occupancy(soup, origin, voxel, n)
-    else:
-        occ = orc.occupancy(v, i, origin, voxel, n)
-    d = orc.distance(v, i, origin, voxel, n, threads=threads)
-    s = orc.sign_parity(v, i, origin, voxel, n, axis=2, threads=threads)
-    dist = (d * s).astype("float32")
-    sec = time.perf_counter() - t0
-    del occ, dist
-    return sec, kind, orc.threads() if threads <= 0 else threads
+    return orc, ref, kind
 
 
-def cpu_baseline(v, i, origin, voxel, n, budget_s=20.0):
-    cells = n[0] * n[1] * n[2]
-    secs = []
-    kind = "port"
-    cores = 1
-    t_start = time.perf_counter()
-    while True:
-        s, kind, cores = cpu_bake(v, i, origin, voxel, n)
-        secs.append(s)
-        if time.perf_counter() - t_start > budget_s * 0.5 or len(secs) >= 3:
+def cpu_sample(meshes, budget_s, seed, orc, ref):
+    """CPU bakes of the workload's meshes in a seeded order until about budget_s seconds.
+    Returns (voxels, seconds, meshes used)."""
+    import numpy as np
+    order = np.random.default_rng(seed).permutation(len(meshes))
+    vox, secs, used = 0, 0.0, 0
+    for k in order:
+        v, i, n = meshes[k]
+        est = n ** 3 * 1.5e-6 * max(1.0, math.log2(max(len(i), 2)) / 17)  # skip bakes far over budget
+        if used and secs + est > budget_s * 1.5:
+            continue
+        secs += cpu_bake(orc, ref, v, i, n)
+        vox += n ** 3
+        used += 1
+        if secs >= budget_s:
             break
-    best = min(secs)
-    return {"value": cells / best, "unit": "voxels/s", "cores": cores, "kind": kind,
-            "sample": f"{len(secs)} full CPU bake(s) of the same mesh and {n[0]}x{n[1]}x{n[2]} grid "
-                      f"(occupancy {'reference triBoxOverlap, 1 thread' if kind == 'reference' else 'oracle port, 1 thread'};"
-                      f" FP64 distance + exact parity, {cores} threads); best {best:.2f} s"}
+    return vox, secs, used
+
+
+def cpu_baseline(meshes, budget_s=20.0, seed=0):
+    orc, ref, kind = cpu_tools()
+    vox, secs, used = cpu_sample(meshes, budget_s, seed, orc, ref)
+    return {"value": vox / secs, "unit": "voxels/s", "cores": orc.threads(), "kind": kind,
+            "sample": f"{used} of the workload's meshes in seeded order, {vox} voxels, {secs:.1f} s "
+                      f"(occupancy: {'the reference triBoxOverlap' if kind == 'reference' else 'oracle port'}, 1 thread;"
+                      f" FP64 distance + exact parity: {orc.threads()} threads)"}
 
 
 def run_reference(args, rank, world):
-    """The reference arm: the CPU bake (the reference's own code path for this bake has no GPU
-    implementation that can run here; its OptiX estimate needs the OptiX SDK)."""
+    """The reference arm: the CPU bake of the workload (the reference's own bake of this path is an
+    OptiX ray-cast estimate and the OptiX SDK is absent, so its CPU occupancy code and the FP64
+    oracle stand in). Each step bakes meshes of the workload in a seeded order for a bounded time."""
     if rank != 0:
         return
-    v, i, origin, voxel, n, cfg = workload(args.workload)
-    cells = n[0] * n[1] * n[2]
-    for _ in range(max(0, min(args.warmup, 1))):
-        cpu_bake(v, i, origin, voxel, n)
-    times = []
-    kind, cores = "port", 1
-    for _ in range(args.steps):
-        s, kind, cores = cpu_bake(v, i, origin, voxel, n)
-        times.append(s)
-        if sum(times) > 150:
-            break
-    tot = sum(times)
-    value = cells * len(times) / tot
+    meshes = batch64_meshes() if args.workload == "batch64" else [sphere256()]
+    orc, ref, kind = cpu_tools()
+    budget = max(5.0, min(25.0, 150.0 / max(args.steps, 1)))
+    for w in range(min(args.warmup, 1)):
+        cpu_sample(meshes, 1.0, 1000 + w, orc, ref)
+    vox, secs, used = 0, 0.0, 0
+    for step in range(args.steps):
+        a, b, c = cpu_sample(meshes, budget, step, orc, ref)
+        vox, secs, used = vox + a, secs + b, used + c
+    value = vox / secs if secs else 0.0
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world,
-            "steps": len(times), "warmup": args.warmup, "ms_per_step": 1000 * tot / len(times),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": cfg,
-            "cpu_baseline": {"value": value, "unit": "voxels/s", "cores": cores, "kind": kind,
-                             "sample": f"{len(times)} full CPU bakes of the workload"},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload},
+            "cpu_baseline": {"value": value, "unit": "voxels/s", "cores": orc.threads(), "kind": kind,
+                             "sample": f"{used} mesh bakes over {args.steps} steps of ~{budget:.0f} s, {vox} voxels"},
             "e2e": {"value": value, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -247,8 +272,129 @@ def sgemm_peak(torch) -> float:
     return best
 
 
-def main():
-    args = parse()
+def new_stats(sdfb):
+    st = sdfb.Stats()
+    st.struct_size = sdfb.C.sizeof(sdfb.Stats)
+    return st
+
+
+def percentile(xs, p):
+    if not xs:
+        return None
+    ys = sorted(xs)
+    k = min(len(ys) - 1, max(0, int(math.ceil(p / 100.0 * len(ys))) - 1))
+    return ys[k]
+
+
+def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, repeat=0.3, workers=48):
+    """The Poisson serving stream. Returns the served record and the request list (for plain)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    reqs, t, news = [], 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            break
+        n = int(rng.choice([32, 64, 128, 256]))
+        if news and rng.uniform() < repeat:
+            key = news[int(rng.integers(len(news)))]
+        else:
+            key = (int(rng.integers(len(base_meshes))), tuple(rng.uniform(-0.03, 0.03, 3).astype(np.float32)))
+            news.append(key)
+        reqs.append((t, key, n))
+    # pinned output slots, sized for the largest grid
+    max_cells = 256 ** 3
+    slots = queue.Queue()
+    slot_bufs = []
+    for k in range(workers):
+        d = torch.empty(max_cells, dtype=torch.float32).pin_memory().numpy()
+        o = torch.empty(max_cells, dtype=torch.uint8).pin_memory().numpy()
+        slot_bufs.append((d, o))
+        slots.put(k)
+    results = [None] * len(reqs)
+    srv = sdfb.Server(ctx, hbm_budget_bytes=150 << 30, max_inflight=64, wave_voxels_log2=25)
+    mesh_cache = {}
+    lock = threading.Lock()
+    work = queue.Queue()
+
+    def mesh_of(key):
+        b, off = key
+        v, f, _ = base_meshes[b]
+        return (v + np.asarray(off, np.float32)).astype(np.float32), f
+
+    def worker():
+        while True:
+            item = work.get()
+            if item is None:
+                return
+            k, arrival = item
+            _, key, n = reqs[k]
+            v, f = mesh_of(key)
+            mid = srv.register(v, f)
+            slot = slots.get()
+            d, o = slot_bufs[slot]
+            g = unit_grid(sdfb, n)
+            cells = g.cells
+            rid = srv.submit(mid, g, d[:cells], o[:cells])
+            done, info = srv.poll(rid, 600000)
+            slots.put(slot)
+            results[k] = (arrival, info["t_submit_ms"] / 1e3, info["t_done_ms"] / 1e3, cells, info["status"])
+
+    threads = [threading.Thread(target=worker, daemon=True) for _ in range(workers)]
+    for th in threads:
+        th.start()
+    # warm the server (first-wave allocations) with one small request outside the stream
+    v0, f0, _ = base_meshes[0]
+    g0 = unit_grid(sdfb, 32)
+    d0, o0 = slot_bufs[0]
+    srv.poll(srv.submit(srv.register(v0, f0), g0, d0[:g0.cells], o0[:g0.cells]), 600000)
+    t0 = time.monotonic()
+    for k, (arr, key, n) in enumerate(reqs):
+        now = time.monotonic() - t0
+        if arr > now:
+            time.sleep(arr - now)
+        work.put((k, t0 + arr))
+    for _ in threads:
+        work.put(None)
+    for th in threads:
+        th.join()
+    srv.close()
+    lat = [r[2] - r[0] for r in results if r]
+    done = [r for r in results if r and r[4] == 0]
+    span = max(r[2] for r in done) - t0
+    vox = sum(r[3] for r in done)
+    return {"requests": len(reqs), "completed": len(done), "new_meshes": len(news),
+            "voxels_per_s": vox / span, "p50_ms": 1e3 * percentile(lat, 50), "p99_ms": 1e3 * percentile(lat, 99),
+            "mean_ms": 1e3 * statistics.mean(lat), "seconds": span, "rate_per_s": rate, "repeat_fraction": repeat,
+            "hbm_budget_gb": 150}, reqs
+
+
+def plain_stream(sdfb, ctx, base_meshes, reqs, seconds):
+    """The same stream served by plain per-request bakes (one at a time, in arrival order) for the
+    arrivals of the first `seconds`."""
+    import numpy as np
+    sub = [r for r in reqs if r[0] < seconds]
+    lat, vox = [], 0
+    t0 = time.monotonic()
+    opts = sdfb.make_opts(sign_mode=sdfb.SIGN_AUTO)
+    for arr, (b, off), n in sub:
+        now = time.monotonic() - t0
+        if arr > now:
+            time.sleep(arr - now)
+        v, f, _ = base_meshes[b]
+        v = (v + np.asarray(off, np.float32)).astype(np.float32)
+        g = unit_grid(sdfb, n)
+        ctx.bake(v, f, g, opts)
+        lat.append(time.monotonic() - t0 - arr)
+        vox += g.cells
+    span = time.monotonic() - t0
+    return {"requests": len(sub), "voxels_per_s": vox / span, "p50_ms": 1e3 * percentile(lat, 50),
+            "p99_ms": 1e3 * percentile(lat, 99), "seconds": span,
+            "note": f"arrivals of the first {seconds:.0f} s of the same stream, one sdfb_bake per request"}
+
+
+def main(argv=None):
+    args = parse(argv)
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
@@ -264,100 +410,109 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
         pg = dist
-    lib_path = sdfb.LIB_PATH
-    if not os.path.exists(lib_path):
+    if not os.path.exists(sdfb.LIB_PATH):
         import build as pkg_build
         pkg_build.build()
     ctx = sdfb.Context(local)
-    v, i, origin, voxel, n, cfg = workload(args.workload)
-    cells = n[0] * n[1] * n[2]
-    grid = sdfb.make_grid(origin, voxel, n)
-    opts = sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY)
     stream = torch.cuda.current_stream()
-    dv = torch.from_numpy(v).cuda()
-    di = torch.from_numpy(i.astype(np.int32)).cuda()
-    dd = torch.empty(cells, dtype=torch.float32, device="cuda")
-    do = torch.empty(cells, dtype=torch.uint8, device="cuda")
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
-    def bake_dev(stats=None):
-        ctx.bake_device(dv.data_ptr(), len(v), di.data_ptr(), len(i), grid, opts, dd.data_ptr(), do.data_ptr(),
-                        stream.cuda_stream, stats)
+    def red_max(x):
+        if not pg:
+            return x
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        return float(t.item())
 
-    def new_stats():
-        st = sdfb.Stats()
-        st.struct_size = sdfb.C.sizeof(sdfb.Stats)
-        return st
+    def red_sum(x):
+        if not pg:
+            return x
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.SUM)
+        return float(t.item())
+
+    meshes = batch64_meshes() if args.workload == "batch64" else [sphere256()]
+    grids = [unit_grid(sdfb, n) for _, _, n in meshes]
+    cells = [g.cells for g in grids]
+    total_cells = sum(cells)
+    opts = sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY)
+    dev_v = [torch.from_numpy(v).cuda() for v, _, _ in meshes]
+    dev_i = [torch.from_numpy(i.astype(np.int32)).cuda() for _, i, _ in meshes]
+    dev_d = [torch.empty(c, dtype=torch.float32, device="cuda") for c in cells]
+    dev_o = [torch.empty(c, dtype=torch.uint8, device="cuda") for c in cells]
+    devm = [(a.data_ptr(), len(v), b.data_ptr(), len(i)) for a, b, (v, i, _) in zip(dev_v, dev_i, meshes)]
+    dptr = [d.data_ptr() for d in dev_d]
+    optr = [o.data_ptr() for o in dev_o]
+
+    def step_batch(stats=None, o=opts):
+        ctx.bake_batch_device(devm, grids, o, dptr, optr, stream.cuda_stream, stats)
+
+    def step_plain(stats_list=None):
+        for k in range(len(meshes)):
+            ctx.bake_device(devm[k][0], devm[k][1], devm[k][2], devm[k][3], grids[k], opts, dptr[k], optr[k],
+                            stream.cuda_stream, stats_list[k] if stats_list else None)
 
     for _ in range(max(args.warmup, 3)):
-        bake_dev()
+        step_batch()
     torch.cuda.synchronize()
+    cst = new_stats(sdfb)
+    step_batch(cst, sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY, count_work=True))  # counting build (untimed)
 
-    # counting build (untimed): exact traversal work of one launch
-    cst = new_stats()
-    ctx.bake_device(dv.data_ptr(), len(v), di.data_ptr(), len(i), grid, sdfb.make_opts(
-        sign_mode=sdfb.SIGN_PARITY, count_work=True), dd.data_ptr(), do.data_ptr(), stream.cuda_stream, cst)
-
-    # timed region
+    # ---- timed region: the batched bake ----
     clocks = ClockSampler(local)
     if pg:
         pg.barrier()
     torch.cuda.synchronize()
     clocks.start()
-    step_ms, dist_ms, launches = [], [], []
+    step_ms, dist_ms, launches, replayed = [], [], [], []
     for _ in range(args.steps):
         flush.fill_(1.0)
-        st = new_stats()
+        st = new_stats(sdfb)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        bake_dev(st)
+        step_batch(st)
         e1.record(stream)
         e1.synchronize()
         step_ms.append(e0.elapsed_time(e1))
         dist_ms.append(st.ms_distance)
         launches.append(st.kernel_launches)
+        replayed.append(st.graph_replayed)
     torch.cuda.synchronize()
     if pg:
         pg.barrier()
     clk = clocks.stop()
-    total_ms = sum(step_ms)
-    if pg:
-        t = torch.tensor([total_ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * cells * args.steps / (total_ms * 1e-3)
+    value, secs = aggregate(total_cells * args.steps, sum(step_ms) / 1e3, red_max, red_sum)
 
-    # e2e through the host-buffer entry point (pinned host memory both ways)
-    hv = torch.from_numpy(v).pin_memory().numpy()
-    hi = torch.from_numpy(i).pin_memory().numpy() if i.dtype == np.uint32 else None
-    if hi is None:
-        hi = torch.from_numpy(i.astype(np.int32)).pin_memory().numpy().view(np.uint32)
-    hd = torch.empty(cells, dtype=torch.float32).pin_memory().numpy().reshape(grid.shape)
-    ho = torch.empty(cells, dtype=torch.uint8).pin_memory().numpy().reshape(grid.shape)
-    lib = ctx.lib
-
-    def bake_host():
-        stt = lib.sdfb_bake(ctx.h, hv.ctypes.data_as(sdfb.C.c_void_p), len(hv), hi.ctypes.data_as(sdfb.C.c_void_p),
-                            len(hi), sdfb.C.byref(grid), sdfb.C.byref(opts), hd.ctypes.data_as(sdfb.C.c_void_p),
-                            ho.ctypes.data_as(sdfb.C.c_void_p), None)
-        if stt != 0:
-            raise sdfb.SdfbError(stt, ctx.error())
-
+    # ---- the plain path on the same meshes (single-mesh calls) ----
     for _ in range(2):
-        bake_host()
+        step_plain()
+    plain_ms = []
+    for _ in range(max(2, args.steps // 3)):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step_plain()
+        e1.record(stream)
+        e1.synchronize()
+        plain_ms.append(e0.elapsed_time(e1))
+    plain_value, _ = aggregate(total_cells * len(plain_ms), sum(plain_ms) / 1e3, red_max, red_sum)
+
+    # ---- e2e: host buffers (pinned) through sdfb_bake_batch ----
+    hmeshes = [(torch.from_numpy(v).pin_memory().numpy(),
+                torch.from_numpy(i.astype(np.int32)).pin_memory().numpy().view(np.uint32)) for v, i, _ in meshes]
+    hd = [torch.empty(c, dtype=torch.float32).pin_memory().numpy().reshape(g.shape) for c, g in zip(cells, grids)]
+    ho = [torch.empty(c, dtype=torch.uint8).pin_memory().numpy().reshape(g.shape) for c, g in zip(cells, grids)]
+    for _ in range(2):
+        ctx.bake_batch(hmeshes, grids, opts, out=(hd, ho))
     e2e_s = []
     for _ in range(max(3, args.steps // 2)):
         flush.fill_(1.0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        bake_host()
+        ctx.bake_batch(hmeshes, grids, opts, out=(hd, ho))
         e2e_s.append(time.perf_counter() - t0)
-    e2e_total = sum(e2e_s)
-    if pg:
-        t = torch.tensor([e2e_total], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = world * cells * len(e2e_s) / e2e_total
+    e2e_value, _ = aggregate(total_cells * len(e2e_s), sum(e2e_s), red_max, red_sum)
+    h2d = int(sum(v.nbytes + i.nbytes for v, i in hmeshes))
 
     if rank != 0:
         if pg:
@@ -365,44 +520,81 @@ def main():
             pg.destroy_process_group()
         return
 
-    # roofline of the distance kernel
+    # ---- the single-mesh 256^3 bake (configs' plain single-mesh GPU bake) ----
+    single = None
+    if args.workload == "batch64":
+        sv, si, sn = sphere256()
+        sg = unit_grid(sdfb, sn)
+        sdv, sdi = torch.from_numpy(sv).cuda(), torch.from_numpy(si.astype(np.int32)).cuda()
+        sdd = torch.empty(sg.cells, dtype=torch.float32, device="cuda")
+        sdo = torch.empty(sg.cells, dtype=torch.uint8, device="cuda")
+        for _ in range(3):
+            ctx.bake_device(sdv.data_ptr(), len(sv), sdi.data_ptr(), len(si), sg, opts, sdd.data_ptr(), sdo.data_ptr(),
+                            stream.cuda_stream)
+        ms = []
+        for _ in range(5):
+            flush.fill_(1.0)
+            st = new_stats(sdfb)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.bake_device(sdv.data_ptr(), len(sv), sdi.data_ptr(), len(si), sg, opts, sdd.data_ptr(), sdo.data_ptr(),
+                            stream.cuda_stream, st)
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        single = {"workload": "displaced-sphere-256 (81,920 triangles, 256^3)", "ms": statistics.median(ms),
+                  "voxels_per_s": sg.cells / (statistics.median(ms) * 1e-3), "ms_distance": st.ms_distance,
+                  "ms_build": st.ms_build, "ms_occupancy": st.ms_occupancy, "ms_sign": st.ms_sign}
+
+    # ---- roofline of the distance kernel ----
     peak = sgemm_peak(torch)
     flops = cst.flops_distance
     mean_dist_ms = statistics.mean(dist_ms)
     achieved = flops / (mean_dist_ms * 1e-3) / 1e12
     roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": None, "kernel": "k_distance", "flops_per_launch": flops,
-                "box_tests": int(cst.box_tests), "tri_tests": int(cst.tri_tests),
-                "kernel_ms": mean_dist_ms,
+                "traffic": None, "kernel": "k_distance", "flops_per_launch": flops, "box_tests": int(cst.box_tests),
+                "tri_tests": int(cst.tri_tests), "kernel_ms": mean_dist_ms,
                 "peak_source": "cuBLAS SGEMM 8192^3 FP32 (TF32 off), best of 5, measured in this run",
-                "algorithmic_bytes_per_launch": cells * 4}
+                "algorithmic_bytes_per_launch": total_cells * 4}
 
-    # precision against FP64 on a seeded sample
+    # ---- precision against FP64 on a seeded sample of every mesh ----
     from oracle.oracle import Oracle
     orc = Oracle()
     rng = np.random.default_rng(0)
-    samp = np.sort(rng.choice(cells, min(cells, 20000), replace=False)).astype(np.int64)
-    d64 = orc.distance(v, i, origin, voxel, n, samples=samp)
-    got = np.abs(hd.reshape(-1)[samp].astype(np.float64))
-    diagv = float(voxel) * float(np.sqrt(n[0] ** 2 + n[1] ** 2 + n[2] ** 2))
-    err = np.abs(got - d64) / diagv
+    errs = []
+    for k, (v, i, n) in enumerate(meshes):
+        samp = np.sort(rng.choice(n ** 3, min(n ** 3, 2000), replace=False)).astype(np.int64)
+        d64 = orc.distance(v, i, (-0.5,) * 3, 1.0 / n, (n, n, n), samples=samp)
+        got = np.abs(hd[k].reshape(-1)[samp].astype(np.float64))
+        errs.append(np.abs(got - d64) / (np.sqrt(3.0)))
+    err = np.concatenate(errs)
 
-    cpu = None if args.no_cpu_baseline else cpu_baseline(v, i, origin, voxel, n)
+    served = None
+    if not args.no_serve and args.workload == "batch64" and world == 1:
+        served, reqs = serve_stream(sdfb, ctx, torch, meshes, args.serve_seconds)
+        served["plain"] = plain_stream(sdfb, ctx, meshes, reqs, min(10.0, args.serve_seconds))
+    cpu = None if args.no_cpu_baseline else cpu_baseline(meshes)
     line = {
         "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": sum(step_ms) / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded meshes generated in-process)",
-        "config": {**cfg, "plain_single_mesh": True, "parallelism": f"replicas x{world}",
-                   "l2": "512 MB L2 flush before every timed step"},
+        "config": {"workload": args.workload, "meshes": len(meshes), "triangles": int(sum(len(i) for _, i, _ in meshes)),
+                   "voxels": int(total_cells), "grids": sorted({n for _, _, n in meshes}), "sign": "parity",
+                   "seed": 2024 if args.workload == "batch64" else 1234, "parallelism": f"replicas x{world}",
+                   "l2": "512 MB L2 flush before every timed step (outputs alone exceed L2)"},
+        "plain": {"value": plain_value, "unit": "voxels/s", "ms_per_step": statistics.mean(plain_ms),
+                  "batched_over_plain": value / plain_value},
         "roofline": roofline,
         "cpu_baseline": cpu,
-        "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": int(v.nbytes + i.nbytes),
-                "d2h_bytes_per_step": int(cells * 5), "ms_per_step": 1000 * e2e_total / len(e2e_s)},
+        "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": int(total_cells * 5), "ms_per_step": 1e3 * statistics.mean(e2e_s)},
         "clocks": clk,
         "gpu_launches": int(sum(launches)),
+        "graph_replayed_steps": int(sum(replayed)),
         "precision": {"max_err_over_diag": float(err.max()), "rms_err_over_diag": float(np.sqrt((err ** 2).mean())),
-                      "samples": int(len(samp)), "reference": "FP64 oracle"},
-        "stages_ms": {"distance": mean_dist_ms},
+                      "samples": int(len(err)), "reference": "FP64 oracle"},
+        "served": served,
+        "single_mesh": single,
     }
     print(json.dumps(line), flush=True)
     if pg:

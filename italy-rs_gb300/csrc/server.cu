@@ -42,12 +42,20 @@ double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-uint64_t fnv1a(const void *p, size_t n, uint64_t h) {
+// Content hash of a mesh (FNV-1a over 8-byte words, then a final avalanche).
+uint64_t content_hash(const void *p, size_t n, uint64_t h) {
   const uint8_t *b = static_cast<const uint8_t *>(p);
-  for (size_t i = 0; i < n; ++i) {
-    h ^= b[i];
-    h *= 0x100000001b3ull;
+  size_t i = 0;
+  for (; i + 8 <= n; i += 8) {
+    uint64_t w;
+    std::memcpy(&w, b + i, 8);
+    h = (h ^ w) * 0x100000001b3ull;
+    h ^= h >> 29;
   }
+  for (; i < n; ++i) h = (h ^ b[i]) * 0x100000001b3ull;
+  h ^= h >> 33;
+  h *= 0xff51afd7ed558ccdull;
+  h ^= h >> 33;
   return h;
 }
 
@@ -436,9 +444,9 @@ sdfb_status sdfb_mesh_register(sdfb_server *srv, const float *verts, uint32_t nu
   if (num_tris == 0 || num_verts == 0) return srv->fail(SDFB_ERR_BAD_MESH, "mesh has no triangles");
   for (size_t k = 0; k < size_t(num_tris) * 3; ++k)
     if (idx[k] >= num_verts) return srv->fail(SDFB_ERR_BAD_MESH, "triangle index out of range");
-  uint64_t h = fnv1a(verts, size_t(num_verts) * 12, 0xcbf29ce484222325ull);
-  h = fnv1a(idx, size_t(num_tris) * 12, h);
-  h = fnv1a(&num_verts, 4, h);
+  uint64_t h = content_hash(verts, size_t(num_verts) * 12, 0xcbf29ce484222325ull);
+  h = content_hash(idx, size_t(num_tris) * 12, h);
+  h = content_hash(&num_verts, 4, h);
   *mesh_id = h;
   {
     std::lock_guard<std::mutex> g(srv->mu);
