@@ -70,6 +70,20 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def reducers(pg, device):
+    """(max, sum) over ranks of one host float, through process group module `pg` (None: one rank)."""
+    import torch
+
+    def red(x, op):
+        if not pg:
+            return x
+        t = torch.tensor([x], device=device, dtype=torch.float64)
+        pg.all_reduce(t, op=op)
+        return float(t.item())
+
+    return (lambda x: red(x, pg.ReduceOp.MAX if pg else None)), (lambda x: red(x, pg.ReduceOp.SUM if pg else None))
+
+
 def aggregate(voxels_per_rank: float, seconds_per_rank: float, all_reduce_max=None, all_reduce_sum=None):
     """Whole-job throughput: the sum of every rank's voxels over the slowest rank's time."""
     secs = all_reduce_max(seconds_per_rank) if all_reduce_max else seconds_per_rank
@@ -417,19 +431,7 @@ def main(argv=None):
     stream = torch.cuda.current_stream()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
-    def red_max(x):
-        if not pg:
-            return x
-        t = torch.tensor([x], device="cuda", dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        return float(t.item())
-
-    def red_sum(x):
-        if not pg:
-            return x
-        t = torch.tensor([x], device="cuda", dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.SUM)
-        return float(t.item())
+    red_max, red_sum = reducers(pg, "cuda")
 
     meshes = batch64_meshes() if args.workload == "batch64" else [sphere256()]
     grids = [unit_grid(sdfb, n) for _, _, n in meshes]

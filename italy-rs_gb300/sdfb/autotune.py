@@ -1,0 +1,166 @@
+"""Autotuner for the bake's launch parameters on the GPU it runs on.
+
+Three parameters of the distance pass trade against each other with the mesh and the grid:
+  * leaf size (triangles per BVH leaf, 1..16): small leaves test fewer triangles per visit but add
+    node tests and stack traffic;
+  * tile shape (the cells one warp walks the BVH for, ids 1..6 = 4x4x2, 8x4x1, 4x4x4, 8x4x2,
+    4x4x8, 8x4x4 cells with 1, 1, 2, 2, 4, 4 cells per lane): bigger tiles share one traversal
+    among more cells but visit the union of their candidates;
+  * traversal stack depth (32 or 64 entries): the shallow stack needs fewer registers but a deep
+    tree overflows it (the bake then reruns that launch with 64).
+
+For each (log2 triangles, log2 grid edge) bucket of a sweep of displaced spheres and grids, the tuner
+times whole device-buffer bakes (CUDA events on the bake's stream, median of `reps`) under a
+coordinate descent over the three parameters, then fills every bucket of the table from the
+nearest measured one and writes "tri_bucket grid_bucket leaf tile stack" lines (tile 0-based) that
+the library reads at context creation (tuning/gb300.tsv beside lib/, or the file SDFB_TUNING names).
+
+    python italy-rs_gb300/sdfb/autotune.py [--out PATH] [--quick]
+"""
+from __future__ import annotations
+
+import argparse
+import datetime
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DEFAULT_OUT = os.path.join(os.path.dirname(HERE), "tuning", "gb300.tsv")
+
+TILES = (1, 2, 3, 4, 5, 6)
+LEAVES = (1, 2, 3, 4, 6, 8)
+STACKS = (32, 64)
+START = (4, 3, 64)  # leaf, tile id (1-based), stack: the built-in defaults
+
+# (icosphere level, grid edge): 1,280 .. 327,680 triangles on 64^3 .. 512^3 grids
+SWEEP = [(3, 64), (3, 128), (3, 256), (4, 64), (4, 128), (4, 256), (5, 128), (5, 256), (5, 512),
+         (6, 128), (6, 256), (6, 512), (7, 128), (7, 256), (7, 512)]
+QUICK = [(4, 128), (6, 256), (7, 256)]
+
+
+def bucket_tris(t: int) -> int:
+    """floor(log2 t), at most 31 (the library's own bucketing of triangle counts)."""
+    b = 0
+    while b < 31 and (2 << b) <= t:
+        b += 1
+    return b
+
+
+def bucket_grid(n: int) -> int:
+    """floor(log2 n) - 4, clamped to 0..7 (the library's own bucketing of the longest grid edge)."""
+    b = 0
+    while b < 20 and (2 << b) <= n:
+        b += 1
+    return max(0, min(7, b - 4))
+
+
+def fill_table(measured: dict) -> dict:
+    """Every (tri bucket 0..31, grid bucket 0..7) from the nearest measured bucket: distance
+    |d tri| + 2 |d grid| (the grid edge moves the work per tile more than the triangle count does),
+    ties to the larger bucket."""
+    table = {}
+    keys = sorted(measured)
+    for tb in range(32):
+        for nb in range(8):
+            best = min(keys, key=lambda k: (abs(k[0] - tb) + 2 * abs(k[1] - nb), -k[0], -k[1]))
+            table[(tb, nb)] = measured[best]
+    return table
+
+
+def write_table(path: str, table: dict, measured: dict, times: dict, header: list[str]):
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    with open(path, "w") as f:
+        for h in header:
+            f.write(f"# {h}\n")
+        f.write("# tri_bucket grid_bucket leaf tile(0-based) stack\n")
+        for (tb, nb), (leaf, tile, stack) in sorted(table.items()):
+            note = f"  # measured {times[(tb, nb)]:.3f} ms" if (tb, nb) in measured else ""
+            f.write(f"{tb} {nb} {leaf} {tile - 1} {stack}{note}\n")
+
+
+def _time_bake(ctx, torch, sdfb, dev, grid, params, reps: int) -> float:
+    leaf, tile, stack = params
+    opts = sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY, leaf_size=leaf, tile=tile, stack_depth=stack)
+    stream = torch.cuda.current_stream()
+    dv, nv, di, nt, dd, do = dev
+    ctx.bake_device(dv, nv, di, nt, grid, opts, dd, do, stream.cuda_stream)  # warm-up
+    times = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.bake_device(dv, nv, di, nt, grid, opts, dd, do, stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    times.sort()
+    return times[len(times) // 2]
+
+
+def tune_case(ctx, torch, sdfb, dev, grid, reps: int, log=print):
+    """Coordinate descent: tile, then leaf, then stack, then tile again. Returns (params, ms)."""
+    cache = {}
+
+    def t(p):
+        if p not in cache:
+            cache[p] = _time_bake(ctx, torch, sdfb, dev, grid, p, reps)
+        return cache[p]
+
+    best = START
+    for axis, values in ((1, TILES), (0, LEAVES), (2, STACKS), (1, TILES)):
+        for v in values:
+            p = list(best)
+            p[axis] = v
+            p = tuple(p)
+            if t(p) < t(best):
+                best = p
+    log(f"    {len(cache)} configurations, best leaf {best[0]} tile {best[1]} stack {best[2]}: {t(best):.3f} ms "
+        f"(defaults {t(START):.3f} ms)")
+    return best, t(best)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--out", default=DEFAULT_OUT)
+    ap.add_argument("--quick", action="store_true", help="three buckets only")
+    ap.add_argument("--reps", type=int, default=3)
+    args = ap.parse_args(argv)
+
+    sys.path.insert(0, os.path.dirname(HERE))
+    import numpy as np
+    import torch
+
+    import sdfb
+    from sdfb import meshgen
+
+    os.environ["SDFB_TUNING"] = os.devnull  # tune from the built-in defaults, not an older table
+    ctx = sdfb.Context(0)
+    measured, times = {}, {}
+    meshes = {}
+    for level, n in (QUICK if args.quick else SWEEP):
+        if level not in meshes:
+            meshes[level] = meshgen.displaced_icosphere(level, 0.4, 100 + level)
+        v, f = meshes[level]
+        grid = sdfb.make_grid((-0.5, -0.5, -0.5), 1.0 / n, (n, n, n))
+        dv = torch.from_numpy(np.ascontiguousarray(v, np.float32)).cuda()
+        di = torch.from_numpy(np.ascontiguousarray(f, np.int32)).cuda()
+        dd = torch.empty(grid.cells, dtype=torch.float32, device="cuda")
+        do = torch.empty(grid.cells, dtype=torch.uint8, device="cuda")
+        key = (bucket_tris(len(f)), bucket_grid(n))
+        print(f"  {len(f):>7} triangles, {n}^3 grid -> bucket {key}", flush=True)
+        params, ms = tune_case(ctx, torch, sdfb, (dv.data_ptr(), len(v), di.data_ptr(), len(f),
+                                                  dd.data_ptr(), do.data_ptr()), grid, args.reps)
+        if key not in measured or ms < times[key]:
+            measured[key], times[key] = params, ms
+        del dv, di, dd, do
+    table = fill_table(measured)
+    header = [f"written by italy-rs_gb300/sdfb/autotune.py{' --quick' if args.quick else ''} on "
+              f"{torch.cuda.get_device_name(0)}, {datetime.date.today().isoformat()}",
+              f"{len(measured)} buckets measured (displaced icospheres, parity sign, median of {args.reps}); "
+              f"the rest filled from the nearest"]
+    write_table(args.out, table, measured, times, header)
+    print(f"wrote {args.out}")
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

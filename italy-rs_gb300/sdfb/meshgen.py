@@ -255,12 +255,12 @@ def soup_with_holes(seed: int = 4321, spheres: int = 5, sphere_level: int = 6, t
 
 def mesh_for_count(target: int, seed: int) -> tuple[np.ndarray, np.ndarray]:
     """A displaced icosphere or torus (seeded coin) with about `target` triangles in [-0.5, 0.5]^3.
-    Icospheres take the level whose count 20 * 4**L is nearest in log scale; tori take nu x nv
-    (aspect 3:1) with 2 nu nv ~= target."""
+    Icospheres take the level whose count 20 * 4**L is nearest in log scale, kept within levels 3..7
+    (1,280 .. 327,680 triangles); tori take nu x nv (aspect 3:1) with 2 nu nv ~= target."""
     rng = np.random.default_rng(seed)
     if rng.uniform() < 0.5:
         level = int(round(math.log(max(target, 20) / 20.0, 4)))
-        level = max(1, min(level, 8))
+        level = max(3, min(level, 7))  # 1,280 .. 327,680 triangles: inside [1e3, 1e6]
         return displaced_icosphere(level, 0.35, int(rng.integers(1 << 30)))
     nv = max(3, int(round(math.sqrt(target / 6.0))))
     nu = max(3, int(round(target / (2.0 * nv))))
