@@ -238,6 +238,24 @@ sdfb_status sdfb_poll(sdfb_server *srv, uint64_t request_id, int32_t timeout_ms,
 /* Text of the server's last error. */
 const char *sdfb_server_last_error(const sdfb_server *srv);
 
+/* ---- occupancy without allocation (no counterpart in the reference) ---------------------- */
+
+/* Dense occupancy -- the same SAT rule and result as sdfb_bake's occ_out -- for callers that may
+ * not allocate device memory: plugins whose host application owns every device allocation,
+ * processes held to a fixed device-memory quota, and latency-bound loops that must avoid the
+ * allocator and cudaFree's device-wide synchronisation. All buffers are device memory supplied by
+ * the caller;
+ * work is enqueued on `stream` (a cudaStream_t, NULL = the legacy default stream) and not waited
+ * for. Working memory is one fixed device array inside the library (about 12 MiB, held on every
+ * device that loads the library until the process exits), so:
+ *   - meshes above 1,048,576 triangles are rejected with SDFB_ERR_INVALID_ARGUMENT;
+ *   - the first call on each device sets up the array's address and must come before any stream
+ *     capture on that device;
+ *   - calls whose work overlaps on the GPU share the array and race; order them on one stream. */
+sdfb_status sdfb_occupancy_noalloc(const float *d_verts, uint32_t num_verts, const uint32_t *d_idx,
+                                   uint32_t num_tris, const sdfb_grid_desc *grid, uint8_t *d_occ_out,
+                                   void *stream);
+
 #ifdef __cplusplus
 }
 #endif

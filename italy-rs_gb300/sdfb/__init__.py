@@ -114,6 +114,7 @@ SIGNATURES = {
     "sdfb_submit": (_i32, [_P, _u64, C.POINTER(GridDesc), C.POINTER(Opts), _P, _P, C.POINTER(_u64)]),
     "sdfb_poll": (_i32, [_P, _u64, _i32, C.POINTER(_i32), C.POINTER(RequestInfo)]),
     "sdfb_server_last_error": (C.c_char_p, [_P]),
+    "sdfb_occupancy_noalloc": (_i32, [_P, _u32, _P, _u32, C.POINTER(GridDesc), _P, _P]),
 }
 
 _lib = None
