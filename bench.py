@@ -66,6 +66,14 @@ def parse(argv=None):
     return ap.parse_args(argv)
 
 
+_T0 = time.monotonic()
+
+
+def stage(name: str):
+    """Progress on stderr (stdout carries only the result line)."""
+    print(f"[bench {time.monotonic() - _T0:8.1f} s] {name}", file=sys.stderr, flush=True)
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -336,6 +344,8 @@ def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, re
         v, f, _ = base_meshes[b]
         return (v + np.asarray(off, np.float32)).astype(np.float32), f
 
+    failures = []
+
     def worker():
         while True:
             item = work.get()
@@ -344,15 +354,28 @@ def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, re
             k, arrival = item
             _, key, n = reqs[k]
             v, f = mesh_of(key)
-            mid = srv.register(v, f)
             slot = slots.get()
-            d, o = slot_bufs[slot]
-            g = unit_grid(sdfb, n)
-            cells = g.cells
-            rid = srv.submit(mid, g, d[:cells], o[:cells])
-            done, info = srv.poll(rid, 600000)
-            slots.put(slot)
-            results[k] = (arrival, info["t_submit_ms"] / 1e3, info["t_done_ms"] / 1e3, cells, info["status"])
+            try:
+                d, o = slot_bufs[slot]
+                g = unit_grid(sdfb, n)
+                cells = g.cells
+                for attempt in range(3):  # a mesh evicted between register and submit is registered again
+                    mid = srv.register(v, f)
+                    try:
+                        rid = srv.submit(mid, g, d[:cells], o[:cells])
+                        break
+                    except sdfb.SdfbError as e:
+                        if e.status != sdfb.ERR_NOT_FOUND or attempt == 2:
+                            raise
+                done, info = srv.poll(rid, 120000)
+                if not done:
+                    raise RuntimeError(f"request {k} not done after 120 s")
+                results[k] = (arrival, info["t_submit_ms"] / 1e3, info["t_done_ms"] / 1e3, cells, info["status"])
+            except Exception as e:  # recorded and reported; the stream goes on
+                with lock:
+                    failures.append(f"{type(e).__name__}: {e}")
+            finally:
+                slots.put(slot)
 
     threads = [threading.Thread(target=worker, daemon=True) for _ in range(workers)]
     for th in threads:
@@ -361,7 +384,7 @@ def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, re
     v0, f0, _ = base_meshes[0]
     g0 = unit_grid(sdfb, 32)
     d0, o0 = slot_bufs[0]
-    srv.poll(srv.submit(srv.register(v0, f0), g0, d0[:g0.cells], o0[:g0.cells]), 600000)
+    srv.poll(srv.submit(srv.register(v0, f0), g0, d0[:g0.cells], o0[:g0.cells]), 120000)
     t0 = time.monotonic()
     for k, (arr, key, n) in enumerate(reqs):
         now = time.monotonic() - t0
@@ -373,11 +396,15 @@ def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, re
     for th in threads:
         th.join()
     srv.close()
+    if failures:
+        print(f"serve_stream: {len(failures)} requests failed, first: {failures[0]}", file=sys.stderr)
     lat = [r[2] - r[0] for r in results if r]
     done = [r for r in results if r and r[4] == 0]
+    if not done:
+        raise RuntimeError(f"serve_stream: no request completed ({len(failures)} failed)")
     span = max(r[2] for r in done) - t0
     vox = sum(r[3] for r in done)
-    return {"requests": len(reqs), "completed": len(done), "new_meshes": len(news),
+    return {"requests": len(reqs), "completed": len(done), "failed": len(reqs) - len(done), "new_meshes": len(news),
             "voxels_per_s": vox / span, "p50_ms": 1e3 * percentile(lat, 50), "p99_ms": 1e3 * percentile(lat, 99),
             "mean_ms": 1e3 * statistics.mean(lat), "seconds": span, "rate_per_s": rate, "repeat_fraction": repeat,
             "hbm_budget_gb": 150}, reqs
@@ -433,7 +460,9 @@ def main(argv=None):
 
     red_max, red_sum = reducers(pg, "cuda")
 
+    stage("generating meshes")
     meshes = batch64_meshes() if args.workload == "batch64" else [sphere256()]
+    stage(f"{len(meshes)} meshes, {sum(len(i) for _, i, _ in meshes)} triangles")
     grids = [unit_grid(sdfb, n) for _, _, n in meshes]
     cells = [g.cells for g in grids]
     total_cells = sum(cells)
@@ -454,11 +483,14 @@ def main(argv=None):
             ctx.bake_device(devm[k][0], devm[k][1], devm[k][2], devm[k][3], grids[k], opts, dptr[k], optr[k],
                             stream.cuda_stream, stats_list[k] if stats_list else None)
 
+    stage("warm-up")
     for _ in range(max(args.warmup, 3)):
         step_batch()
     torch.cuda.synchronize()
     cst = new_stats(sdfb)
+    stage("counting build")
     step_batch(cst, sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY, count_work=True))  # counting build (untimed)
+    stage("timed steps")
 
     # ---- timed region: the batched bake ----
     clocks = ClockSampler(local)
@@ -485,6 +517,7 @@ def main(argv=None):
     clk = clocks.stop()
     value, secs = aggregate(total_cells * args.steps, sum(step_ms) / 1e3, red_max, red_sum)
 
+    stage(f"batched: {statistics.mean(step_ms):.1f} ms per step")
     # ---- the plain path on the same meshes (single-mesh calls) ----
     for _ in range(2):
         step_plain()
@@ -499,6 +532,7 @@ def main(argv=None):
         plain_ms.append(e0.elapsed_time(e1))
     plain_value, _ = aggregate(total_cells * len(plain_ms), sum(plain_ms) / 1e3, red_max, red_sum)
 
+    stage(f"plain: {statistics.mean(plain_ms):.1f} ms per step")
     # ---- e2e: host buffers (pinned) through sdfb_bake_batch ----
     hmeshes = [(torch.from_numpy(v).pin_memory().numpy(),
                 torch.from_numpy(i.astype(np.int32)).pin_memory().numpy().view(np.uint32)) for v, i, _ in meshes]
@@ -515,6 +549,7 @@ def main(argv=None):
         e2e_s.append(time.perf_counter() - t0)
     e2e_value, _ = aggregate(total_cells * len(e2e_s), sum(e2e_s), red_max, red_sum)
     h2d = int(sum(v.nbytes + i.nbytes for v, i in hmeshes))
+    stage(f"e2e: {1e3 * statistics.mean(e2e_s):.1f} ms per step")
 
     if rank != 0:
         if pg:
@@ -548,14 +583,17 @@ def main(argv=None):
                   "voxels_per_s": sg.cells / (statistics.median(ms) * 1e-3), "ms_distance": st.ms_distance,
                   "ms_build": st.ms_build, "ms_occupancy": st.ms_occupancy, "ms_sign": st.ms_sign}
 
+    stage("single mesh done" if single else "no single-mesh leg")
     # ---- roofline of the distance kernel ----
     peak = sgemm_peak(torch)
+    stage(f"SGEMM peak {peak:.1f} TFLOP/s")
     flops = cst.flops_distance
     mean_dist_ms = statistics.mean(dist_ms)
     achieved = flops / (mean_dist_ms * 1e-3) / 1e12
     roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": None, "kernel": "k_distance", "flops_per_launch": flops, "box_tests": int(cst.box_tests),
-                "tri_tests": int(cst.tri_tests), "kernel_ms": mean_dist_ms,
+                "traffic": None, "kernel": "k_distance (+ k_distance_deferred)", "flops_per_launch": flops,
+                "box_tests": int(cst.box_tests), "tri_tests": int(cst.tri_tests),
+                "plane_tests": int(cst.plane_tests), "tiles_deferred": int(cst.tiles_deferred), "kernel_ms": mean_dist_ms,
                 "peak_source": "cuBLAS SGEMM 8192^3 FP32 (TF32 off), best of 5, measured in this run",
                 "algorithmic_bytes_per_launch": total_cells * 4}
 
@@ -570,12 +608,16 @@ def main(argv=None):
         got = np.abs(hd[k].reshape(-1)[samp].astype(np.float64))
         errs.append(np.abs(got - d64) / (np.sqrt(3.0)))
     err = np.concatenate(errs)
+    stage(f"precision: max {err.max():.3g} x diag")
 
     served = None
     if not args.no_serve and args.workload == "batch64" and world == 1:
         served, reqs = serve_stream(sdfb, ctx, torch, meshes, args.serve_seconds)
+        stage(f"served: {served['completed']}/{served['requests']} in {served['seconds']:.1f} s")
         served["plain"] = plain_stream(sdfb, ctx, meshes, reqs, min(10.0, args.serve_seconds))
+        stage("plain stream done")
     cpu = None if args.no_cpu_baseline else cpu_baseline(meshes)
+    stage("CPU baseline done")
     line = {
         "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sum(step_ms) / args.steps, "higher_is_better": True, "scaling": "weak",

@@ -79,7 +79,10 @@ typedef struct sdfb_opts {
   int32_t no_distance;    /* 1: occupancy only (dist_out may be NULL) */
   int32_t count_work;     /* 1: count traversal work into stats (a slower, instrumented kernel) */
   int32_t stack_depth;    /* traversal stack entries, 32 or 64, 0: autotuned table */
-  int32_t reserved[7];
+  int32_t step_budget;    /* a distance tile's walk checks every this many steps whether all tiles
+                             are handed out, and if so leaves its tile to a second pass where a
+                             whole block finishes it; 0: autotuned table, -1: never */
+  int32_t reserved[6];
 } sdfb_opts;
 
 /* Per-call statistics, filled when the pointer is non-null. Times are CUDA-event times on the
@@ -107,6 +110,9 @@ typedef struct sdfb_stats {
   uint64_t kernel_launches; /* kernels this call launched */
   uint64_t gwn_fp64_cells;  /* GWN: cells whose winding number was evaluated in FP64 (band + ambiguous) */
   uint64_t graph_replayed;  /* 1 when the launch sequence was replayed from a CUDA graph */
+  uint64_t tiles_deferred;  /* distance tiles that exceeded the step budget and were finished by a
+                               whole block in the second distance pass */
+  uint64_t plane_tests;     /* count_work: cell-plane lower-bound tests (lanes) that screen triangles */
   uint64_t reserved[2];
 } sdfb_stats;
 
@@ -163,6 +169,73 @@ sdfb_status sdfb_voxelize_sparse(sdfb_ctx *ctx, const float *positions, uint32_t
                                  const float bounds_max[3], int32_t resolution, int32_t *cells_out, uint64_t cap,
                                  uint64_t *count, float origin_out[3], float *voxel_out);
 
+/* ---- per-cell materials (src/convert/sdf_baker.cpp:42-128, src/convert/voxelize.cpp:12-107) */
+
+/* One RGBA8 texture (TextureAsset, src/io/mesh_asset.h:10-15). */
+typedef struct sdfb_texture {
+  const uint8_t *rgba; /* width * height * 4 bytes, rows of texels */
+  int32_t width;
+  int32_t height;
+  int32_t srgb;        /* nonzero: the texels are sRGB-encoded and are decoded to linear */
+  int32_t reserved;
+} sdfb_texture;
+
+/* The MaterialAsset fields the bake reads (src/io/mesh_asset.h:17-31). */
+typedef struct sdfb_material {
+  float base_color[3];
+  float metallic;
+  float roughness;
+  int32_t base_color_texture; /* index into the texture list; out of range = no texture */
+} sdfb_material;
+
+/* A MeshAsset's materials: per triangle t the material triangle_material[t] (material 0 past the
+ * end of the list or of the material table), its base colour modulated by the texture texel
+ * nearest the mean of the triangle's three uvs (uvs[3t..3t+2], wrapped to [0, 1)) when the
+ * material names a texture and the triangle has uvs. */
+typedef struct sdfb_materials {
+  uint32_t struct_size;      /* sizeof(sdfb_materials) */
+  uint32_t num_materials;    /* >= 1 */
+  const sdfb_material *materials;
+  const uint32_t *triangle_material; /* may be NULL */
+  uint64_t num_triangle_material;
+  const float *uvs;          /* 2 floats per soup vertex (3 per triangle); may be NULL */
+  uint64_t num_uvs;          /* uv pairs */
+  const sdfb_texture *textures;
+  uint32_t num_textures;
+  uint32_t reserved;
+} sdfb_materials;
+
+/* Per-cell material of the SDF grid (bakePerCellMaterial, src/convert/sdf_baker.cpp:76-128):
+ * every triangle of the soup (9 floats each) that overlaps a cell by the occupancy rule adds its
+ * material to the cell in triangle order; a cell's base colour, metallic and roughness are the
+ * means, and a cell without a triangle keeps (1, 1, 1), 0 and 1. The grid is the bake's (e.g. from
+ * sdfb_grid_from_bounds_res or sdfb_bake_soup). Outputs are host buffers of nx * ny * nz cells,
+ * x fastest; base_color_out holds 3 floats per cell. Any output may be NULL. */
+sdfb_status sdfb_bake_materials(sdfb_ctx *ctx, const float *positions, uint32_t num_tris, const sdfb_grid_desc *grid,
+                                const sdfb_materials *materials, float *base_color_out, float *metallic_out,
+                                float *roughness_out);
+
+/* sdfb_voxelize_sparse plus VoxelGrid::colors (src/convert/voxelize.cpp:78-104): colors_out gets
+ * 3 floats per written cell, the mean base colour of the triangles overlapping it. */
+sdfb_status sdfb_voxelize_sparse_colors(sdfb_ctx *ctx, const float *positions, uint32_t num_tris,
+                                        const float bounds_min[3], const float bounds_max[3], int32_t resolution,
+                                        const sdfb_materials *materials, int32_t *cells_out, float *colors_out,
+                                        uint64_t cap, uint64_t *count, float origin_out[3], float *voxel_out);
+
+/* ---- consumer check (src/render/kernels/pathtracer.cu:587-613, 684-702, 740-787) --------- */
+
+/* The renderer's trilinear sample of a baked grid (sampleSdf, pathtracer.cu:684-702) at
+ * num_points points (3 floats each). `dist` is the grid's host distance buffer (nx*ny*nz, x
+ * fastest); every axis needs at least 2 cells. */
+sdfb_status sdfb_sample_sdf(sdfb_ctx *ctx, const sdfb_grid_desc *grid, const float *dist, const float *points,
+                            uint64_t num_points, float *out);
+
+/* The renderer's sphere-traced intersection with a baked grid (__intersection__sdf,
+ * pathtracer.cu:740-787): per ray (origin, direction: 6 floats) the hit distance it reports within
+ * [tmin, tmax], or -1 when it reports none. */
+sdfb_status sdfb_trace_sdf(sdfb_ctx *ctx, const sdfb_grid_desc *grid, const float *dist, const float *rays,
+                           uint64_t num_rays, float tmin, float tmax, float *t_out);
+
 /* ---- mesh utilities (src/io/mesh_weld.cpp:26-48, src/io/mesh_validate.cpp:21-59) -------- */
 
 /* Welds positions on the max(|extent| * 1e-5, 1e-6) lattice; welded_out gets one index per
@@ -173,6 +246,17 @@ sdfb_status sdfb_weld(sdfb_ctx *ctx, const float *positions, uint32_t num_positi
  * used once (boundary) or more than twice (non-manifold); degenerate triangles are skipped. */
 sdfb_status sdfb_is_watertight(sdfb_ctx *ctx, const uint32_t *welded_idx, uint32_t num_tris, int32_t *watertight,
                                uint64_t *boundary_edges, uint64_t *nonmanifold_edges);
+
+/* The same two on the device, for soups already in device memory (d_positions: 3 floats per
+ * position; d_welded_out / d_welded_idx: device uint32). Work runs on `stream` (NULL = the
+ * context's stream); the calls return after it completes. Same numbering and verdicts as above;
+ * a mesh without triangles is not watertight (mesh_validate.cpp:23-26). */
+sdfb_status sdfb_weld_device(sdfb_ctx *ctx, const float *d_positions, uint32_t num_positions,
+                             const float bounds_min[3], const float bounds_max[3], uint32_t *d_welded_out,
+                             uint32_t *num_unique, void *stream);
+sdfb_status sdfb_is_watertight_device(sdfb_ctx *ctx, const uint32_t *d_welded_idx, uint32_t num_tris,
+                                      int32_t *watertight, uint64_t *boundary_edges, uint64_t *nonmanifold_edges,
+                                      void *stream);
 
 /* ---- batched bake -------------------------------------------------------------------------- */
 

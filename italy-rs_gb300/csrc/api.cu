@@ -74,8 +74,9 @@ sdfb_ctx::~sdfb_ctx() {
 }
 
 DevBuf *sdfb_ctx::all_bufs(int i) {
-  DevBuf *b[] = {&in_verts, &in_idx,   &in_verts2, &in_idx2,    &in_caps,   &in_capidx,
-                 &out_dist, &out_occ,  &first_tri, &sparse_tmp, &sparse_out};
+  DevBuf *b[] = {&in_verts, &in_idx,   &in_verts2, &in_idx2,    &in_caps,   &in_capidx, &out_dist,
+                 &out_occ,  &first_tri, &sparse_tmp, &sparse_out, &mat_rec,  &mat_in,    &mat_tri,
+                 &hit_keys, &hit_vals,  &hit_alt,   &mat_cells, &cons_grid, &cons_io,    &weld_tmp};
   return i < int(sizeof b / sizeof b[0]) ? b[i] : nullptr;
 }
 
@@ -395,36 +396,39 @@ sdfb_status sdfb_bake_soup(sdfb_ctx *ctx, const float *positions, uint32_t num_t
   cudaSetDevice(ctx->device);
   const sdfb_opts o = opts_or_default(opts);
   const uint32_t V = 3 * num_tris;
-  // Weld (first occurrence kept) for the watertight gate and for a crack-free crossing mesh.
-  std::vector<uint32_t> welded(V);
-  const uint32_t U = weld_positions(positions, V, bounds_min, bounds_max, welded.data());
-  std::vector<float> uniq(size_t(U) * 3);
-  std::vector<uint8_t> seen(U, 0);
-  for (uint32_t i = 0; i < V; ++i)
-    if (!seen[welded[i]]) {
-      seen[welded[i]] = 1;
-      std::memcpy(&uniq[size_t(welded[i]) * 3], positions + size_t(i) * 3, 12);
-    }
-  std::vector<PlanMesh> ms(1);
-  PlanMesh &p = ms[0];
-  if (o.sign_mode == SDFB_SIGN_AUTO) {
-    uint64_t b, m;
-    p.watertight = watertight_flag(welded.data(), num_tris, &b, &m) == 1 ? 1 : 0;
-    p.sign = p.watertight ? kSignParity : kSignGwn;
-  } else {
-    p.sign = resolve_sign(o, nullptr, 0, nullptr, 0, &p.watertight);
-  }
-  std::vector<uint32_t> ident(V);
-  for (uint32_t i = 0; i < V; ++i) ident[i] = i;
   const cudaStream_t st = ctx->stream;
   const uint64_t cells = uint64_t(grid_out->nx) * grid_out->ny * grid_out->nz;
   const bool want_dist = dist_out && !o.no_distance, want_occ = occ_out && !o.no_occupancy;
+  std::vector<uint32_t> ident(V);
+  for (uint32_t i = 0; i < V; ++i) ident[i] = i;
   ENSURE(ctx->in_verts, size_t(V) * 12);
   ENSURE(ctx->in_idx, size_t(V) * 4);
   if (want_dist) ENSURE(ctx->out_dist, cells * 4);
   if (want_occ) ENSURE(ctx->out_occ, cells);
   CK(cudaMemcpyAsync(ctx->in_verts.p, positions, size_t(V) * 12, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(ctx->in_idx.p, ident.data(), size_t(V) * 4, cudaMemcpyHostToDevice, st));
+  // Weld on the device (first occurrence kept) for the watertight gate and for a crack-free
+  // crossing mesh: welded indices in in_idx2, unique positions in in_verts2.
+  ENSURE(ctx->in_idx2, size_t(V) * 4);
+  ENSURE(ctx->in_verts2, size_t(V) * 12);
+  ENSURE(ctx->weld_tmp, std::max(weld_temp_bytes(V) + size_t(V) * 4 + 256, watertight_temp_bytes(num_tris)));
+  uint32_t *d_welded = static_cast<uint32_t *>(ctx->in_idx2.p);
+  uint32_t *d_first = reinterpret_cast<uint32_t *>(static_cast<char *>(ctx->weld_tmp.p) + weld_temp_bytes(V));
+  uint32_t U = 0;
+  CK(weld_device(static_cast<const float *>(ctx->in_verts.p), V, weld_cell(bounds_min, bounds_max), d_welded, d_first,
+                 ctx->weld_tmp.p, weld_temp_bytes(V), &U, ctx->num_sms, st));
+  CK(gather_unique(static_cast<const float *>(ctx->in_verts.p), d_first, U, static_cast<float *>(ctx->in_verts2.p),
+                   ctx->num_sms, st));
+  std::vector<PlanMesh> ms(1);
+  PlanMesh &p = ms[0];
+  if (o.sign_mode == SDFB_SIGN_AUTO) {
+    uint64_t b = 0, m = 0;
+    CK(watertight_device(d_welded, num_tris, U, ctx->weld_tmp.p, ctx->weld_tmp.cap, &b, &m, ctx->num_sms, st));
+    p.watertight = (b == 0 && m == 0) ? 1 : 0;
+    p.sign = p.watertight ? kSignParity : kSignGwn;
+  } else {
+    p.sign = resolve_sign(o, nullptr, 0, nullptr, 0, &p.watertight);
+  }
   p.verts = static_cast<const float *>(ctx->in_verts.p);
   p.idx = static_cast<const uint32_t *>(ctx->in_idx.p);
   p.V = V;
@@ -433,14 +437,16 @@ sdfb_status sdfb_bake_soup(sdfb_ctx *ctx, const float *positions, uint32_t num_t
   p.dist = want_dist ? static_cast<float *>(ctx->out_dist.p) : nullptr;
   p.occ = want_occ ? static_cast<uint8_t *>(ctx->out_occ.p) : nullptr;
   if (p.sign == kSignGwn && want_dist) {
+    // the caps are built on the host from the welded mesh
+    std::vector<uint32_t> welded(V);
+    std::vector<float> uniq(size_t(U) * 3);
+    CK(cudaMemcpyAsync(welded.data(), d_welded, size_t(V) * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(uniq.data(), ctx->in_verts2.p, size_t(U) * 12, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
     std::vector<CapBuild> caps(1);
     build_caps(uniq.data(), U, welded.data(), num_tris, caps[0]);
     if ((s = upload_caps(ctx, st, ms, caps)) != SDFB_OK) return s;
   } else if (p.sign == kSignParity && want_dist) {
-    ENSURE(ctx->in_verts2, size_t(U) * 12);
-    ENSURE(ctx->in_idx2, size_t(V) * 4);
-    CK(cudaMemcpyAsync(ctx->in_verts2.p, uniq.data(), size_t(U) * 12, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(ctx->in_idx2.p, welded.data(), size_t(V) * 4, cudaMemcpyHostToDevice, st));
     p.pverts = static_cast<const float *>(ctx->in_verts2.p);
     p.pidx = static_cast<const uint32_t *>(ctx->in_idx2.p);
     p.pV = U;
@@ -451,6 +457,41 @@ sdfb_status sdfb_bake_soup(sdfb_ctx *ctx, const float *positions, uint32_t num_t
   if (want_dist) CK(cudaMemcpyAsync(dist_out, ctx->out_dist.p, cells * 4, cudaMemcpyDeviceToHost, st));
   if (want_occ) CK(cudaMemcpyAsync(occ_out, ctx->out_occ.p, cells, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  return SDFB_OK;
+}
+
+sdfb_status sdfb_weld_device(sdfb_ctx *ctx, const float *d_positions, uint32_t num_positions,
+                             const float bounds_min[3], const float bounds_max[3], uint32_t *d_welded_out,
+                             uint32_t *num_unique, void *stream) {
+  if (!ctx) return SDFB_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if ((num_positions && (!d_positions || !d_welded_out)) || !bounds_min || !bounds_max || !num_unique)
+    return ctx_fail(ctx, SDFB_ERR_INVALID_ARGUMENT, "null argument");
+  cudaSetDevice(ctx->device);
+  const cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  ENSURE(ctx->weld_tmp, weld_temp_bytes(num_positions));
+  CK(weld_device(d_positions, num_positions, weld_cell(bounds_min, bounds_max), d_welded_out, nullptr, ctx->weld_tmp.p,
+                 ctx->weld_tmp.cap, num_unique, ctx->num_sms, st));
+  return SDFB_OK;
+}
+
+sdfb_status sdfb_is_watertight_device(sdfb_ctx *ctx, const uint32_t *d_welded_idx, uint32_t num_tris,
+                                      int32_t *watertight_out, uint64_t *boundary_edges, uint64_t *nonmanifold_edges,
+                                      void *stream) {
+  if (!ctx) return SDFB_ERR_INVALID_ARGUMENT;
+  ctx->err.clear();
+  if ((num_tris && !d_welded_idx) || !watertight_out) return ctx_fail(ctx, SDFB_ERR_INVALID_ARGUMENT, "null argument");
+  cudaSetDevice(ctx->device);
+  const cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  uint64_t b = 0, m = 0;
+  if (num_tris) {
+    ENSURE(ctx->weld_tmp, watertight_temp_bytes(num_tris));
+    CK(watertight_device(d_welded_idx, num_tris, 0, ctx->weld_tmp.p, ctx->weld_tmp.cap, &b, &m,
+                         ctx->num_sms, st));
+  }
+  *watertight_out = (num_tris && b == 0 && m == 0) ? 1 : 0;  // no triangles: not watertight
+  if (boundary_edges) *boundary_edges = b;
+  if (nonmanifold_edges) *nonmanifold_edges = m;
   return SDFB_OK;
 }
 
@@ -478,6 +519,16 @@ sdfb_status sdfb_voxelize_sparse(sdfb_ctx *ctx, const float *positions, uint32_t
                                  uint64_t *count, float origin_out[3], float *voxel_out) {
   if (!ctx) return SDFB_ERR_INVALID_ARGUMENT;
   ctx->err.clear();
+  return voxelize_sparse_run(ctx, positions, num_tris, bounds_min, bounds_max, resolution, cells_out, cap, count,
+                             origin_out, voxel_out, nullptr, nullptr);
+}
+
+}  // extern "C"
+
+sdfb_status voxelize_sparse_run(sdfb_ctx *ctx, const float *positions, uint32_t num_tris, const float bounds_min[3],
+                                const float bounds_max[3], int32_t resolution, int32_t *cells_out, uint64_t cap,
+                                uint64_t *count, float origin_out[3], float *voxel_out, const uint32_t **d_list,
+                                sdfb_grid_desc *grid_out) {
   if (!positions || !bounds_min || !bounds_max || !count || (cap && !cells_out) || resolution < 1)
     return ctx_fail(ctx, SDFB_ERR_INVALID_ARGUMENT, "null argument or resolution < 1");
   if (uint64_t(resolution) * resolution * resolution >= (1ull << 32))
@@ -499,6 +550,7 @@ sdfb_status sdfb_voxelize_sparse(sdfb_ctx *ctx, const float *positions, uint32_t
   g.nx = g.ny = g.nz = resolution;
   if (origin_out) std::memcpy(origin_out, g.origin, 12);
   if (voxel_out) *voxel_out = voxel;
+  if (grid_out) *grid_out = g;
   *count = 0;
   if (num_tris == 0) return SDFB_OK;
   const uint32_t V = 3 * num_tris;
@@ -556,6 +608,7 @@ sdfb_status sdfb_voxelize_sparse(sdfb_ctx *ctx, const float *positions, uint32_t
   while (bits < 32 && (uint64_t(1) << bits) < num_tris) ++bits;
   CK(sparse_emit(static_cast<const uint8_t *>(ctx->out_occ.p), static_cast<const uint32_t *>(ctx->first_tri.p), cells,
                  total, bits, ctx->sparse_tmp.p, ctx->sparse_tmp.cap, static_cast<uint32_t *>(ctx->out_dist.p), st));
+  if (d_list) *d_list = static_cast<const uint32_t *>(ctx->out_dist.p);
   const uint64_t n = std::min<uint64_t>(total, cap);
   std::vector<uint32_t> lin(n);
   if (n) CK(cudaMemcpyAsync(lin.data(), ctx->out_dist.p, n * 4, cudaMemcpyDeviceToHost, st));
@@ -569,6 +622,8 @@ sdfb_status sdfb_voxelize_sparse(sdfb_ctx *ctx, const float *positions, uint32_t
   }
   return SDFB_OK;
 }
+
+extern "C" {
 
 // ---- batched bake ------------------------------------------------------------------------------
 

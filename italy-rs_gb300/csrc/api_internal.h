@@ -84,10 +84,17 @@ struct GwnInput {
   uint64_t gwn_cells;  // cells of the winding-number meshes (refine list capacity)
 };
 
+// Workspace::misc (256 bytes, zeroed before every bake): error flags at 0, the distance tile
+// counter at 64, work counters at 128 (box, triangle, SAT, plane tests), the deferral counters at
+// 160.
+constexpr size_t kMiscDeferOffset = 160;
+// Traversal steps a distance tile may take before it is deferred to the block-per-tile pass.
+constexpr int kDefaultStepBudget = 1024;
+
 // Device workspace of one bake in flight. The context owns one; the serving loop owns one per
 // stream so consecutive waves overlap.
 struct Workspace {
-  DevBuf batch_buf, bvh, build_tmp, par_tmp, col_start, col_z, col_s, caps_bvh, caps_tmp, misc, gwn_tmp;
+  DevBuf batch_buf, bvh, build_tmp, par_tmp, col_start, col_z, col_s, caps_bvh, caps_tmp, misc, gwn_tmp, defer;
   PinBuf staging;
   cudaEvent_t ev[8] = {};
   uint64_t col_capacity_hint = 0;
@@ -115,11 +122,17 @@ struct sdfb_ctx {
   // inputs / outputs of host-buffer calls
   DevBuf in_verts, in_idx, in_verts2, in_idx2, in_caps, in_capidx, out_dist, out_occ, first_tri, sparse_tmp,
       sparse_out;
+  // materials: the batch record, material tables and texels, per-triangle materials, sorted hits,
+  // per-cell outputs
+  DevBuf mat_rec, mat_in, mat_tri, hit_keys, hit_vals, hit_alt, mat_cells;
+  DevBuf cons_grid, cons_io;  // consumer check: a grid and its queries / results
+  DevBuf weld_tmp;            // device weld / watertight census
   PinBuf staging_small;
   Workspace ws;
   int tuned_leaf[32][8];  // [log2 T][log2 n - 4]
   int tuned_tile[32][8];
   int tuned_stack[32][8];
+  int tuned_budget[32][8];  // distance pass: steps before a tile is deferred (0 = never)
 
   ~sdfb_ctx();
   DevBuf *all_bufs(int i);
@@ -135,6 +148,12 @@ void load_tuning(sdfb_ctx *ctx);
 
 sdfb_status ctx_fail(sdfb_ctx *ctx, sdfb_status st, const char *fmt, ...);
 sdfb_status ctx_cuda(sdfb_ctx *ctx, cudaError_t e, const char *what);
+// sdfb_voxelize_sparse; also returns the device list of the count occupied cells' linear indices
+// (valid until the context's next call) and the grid it used.
+sdfb_status voxelize_sparse_run(sdfb_ctx *ctx, const float *positions, uint32_t num_tris, const float bounds_min[3],
+                                const float bounds_max[3], int32_t resolution, int32_t *cells_out, uint64_t cap,
+                                uint64_t *count, float origin_out[3], float *voxel_out, const uint32_t **d_list,
+                                sdfb_grid_desc *grid_out);
 bool grid_ok(const sdfb_grid_desc *g);
 sdfb::GridDev to_dev(const sdfb_grid_desc &g);
 sdfb_opts opts_or_default(const sdfb_opts *o);

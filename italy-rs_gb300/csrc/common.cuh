@@ -237,8 +237,10 @@ __device__ __forceinline__ float point_tri_dist2(float px, float py, float pz, c
 // point_tri_dist2 = 3 (ap) + 3 x 17 (edge: dot 5, scale 1, p - t e 6, |.|^2 5) + 6 (bp, e3)
 //                 + 2 x 14 (cross 9 + dot 5) + 5 (h) + 2 (h^2 w) + 2 (inside test) = 97
 // box_dist2       = 3 x 2 (sub) + 5 (|d|^2) = 11
+// plane bound     = 3 (ap) + 5 (ap . n) + 2 (h^2 w) = 10
 constexpr int kFlopsPointTri = 97;
 constexpr int kFlopsPointBox = 11;
+constexpr int kFlopsPointPlane = 10;
 
 // ---------------------------------------------------------------------------------------------
 // BVH node (64 bytes): the boxes of both children plus their references, so one 64-byte read

@@ -10,10 +10,23 @@
 // deferred child is pushed as (node, child) and its box is re-tested against the tightened
 // bounds when popped. The stack lives in registers, one entry per lane, read with __shfl_sync.
 //
+// Two passes keep one expensive tile from holding the whole GPU. Cells far inside a closed surface
+// are nearly equidistant to much of it, so their tiles walk a large part of the tree; a single
+// such tile, taken late by one warp, used to run alone for a quarter of the kernel. In pass A a
+// walk looks at the tile counter every `step_budget` steps; once every tile has been handed out
+// (the tail, where a long walk would keep one SM busy while the rest idle) it stops, stores its
+// cells' current bounds (squared distances, upper bounds of the answer) in the output and appends
+// the tile to a deferred list. Pass B
+// gives each deferred tile a whole block: the tree is cut into 2^kSplitBits subtrees below the
+// root, the block's warps take subtrees from a shared counter, each walks its subtree for all the
+// tile's cells starting from the stored bounds, and the warps publish their bounds to shared
+// memory (atomicMin on the float bits, valid for non-negative values) after every subtree.
+//
 // Sign: parity counts the column's crossing heights above each cell (the crossing list is
 // built by parity.cu). Winding-number signs are applied afterwards by gwn.cu, which needs the
 // unsigned distance to find the near-surface band.
 #include <algorithm>
+#include <climits>
 #include <cstdint>
 
 #include "common.cuh"
@@ -23,6 +36,9 @@ namespace sdfb {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kWarpsPerBlock = kThreads / kWarp;
+constexpr int kSplitBits = 5;  // pass B: 32 subtrees per deferred tile
+constexpr float kInf = __builtin_huge_valf();
 
 struct Shape {
   int tx, ty, tz;
@@ -30,206 +46,419 @@ struct Shape {
 constexpr Shape kShapes[] = {{4, 4, 2}, {8, 4, 1}, {4, 4, 4}, {8, 4, 2}, {4, 4, 8}, {8, 4, 4}};
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
-template <int TX, int TY, int TZ, int STACK, bool COUNT>
-__global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a) {
-  constexpr int kLayer = TX * TY;
-  constexpr int kLanesZ = kWarp / kLayer;
-  constexpr int VPL = TZ / kLanesZ;
-  static_assert(kLayer * kLanesZ == kWarp && VPL * kLanesZ == TZ, "tile must cover whole warps");
-  static_assert(STACK == 32 || STACK == 64, "stack depth is one or two registers per lane");
-  const int lane = threadIdx.x & 31;
-  const int lx = lane % TX, ly = (lane / TX) % TY, lz = lane / kLayer;
-  const BatchDev &B = a.batch;
-  unsigned long long box_tests = 0, tri_tests = 0;
+struct WalkStats {
+  unsigned long long box_tests = 0, tri_tests = 0, plane_tests = 0;
   bool overflow = false, corrupt = false;
+};
 
-  for (;;) {
-    unsigned long long tile = 0;
-    if (lane == 0) tile = atomicAdd(a.tile_counter, 1ull);
-    tile = __shfl_sync(kFull, tile, 0);
-    if (tile >= B.total_tiles) break;
+// A tile's cells as one lane sees them.
+template <int TX, int TY, int TZ>
+struct TileCells {
+  static constexpr int kLayer = TX * TY;
+  static constexpr int kLanesZ = kWarp / kLayer;
+  static constexpr int VPL = TZ / kLanesZ;
+  static_assert(kLayer * kLanesZ == kWarp && VPL * kLanesZ == TZ, "tile must cover whole warps");
+  const MeshRec *M;
+  GridDev g;
+  int vx, vy, vz0;  // this lane's column and first z; cell v is at z = vz0 + v * kLanesZ
+  float px, py, pz[VPL];
+  bool active[VPL];
+
+  __device__ __forceinline__ void locate(const BatchDev &B, unsigned long long tile, int lane) {
     const int mesh = find_mesh(B.tile_starts, B.num_meshes, tile);
-    const MeshRec &M = B.recs[mesh];
-    const GridDev g = M.g;
-    const Node *__restrict__ nodes = M.nodes;
-    const TriRec *__restrict__ tris = M.tris;
-    const int num_nodes = M.bvh_nodes, num_tris = M.bvh_tris;
-    // A correct tree expands each inner node at most once per tile and pops at most once per
-    // push; anything longer means a corrupt tree, and the walk stops with an error.
-    const long long step_limit = 2ll * num_nodes + 64;
+    M = &B.recs[mesh];
+    g = M->g;
     const unsigned long long local = tile - B.tile_starts[mesh];
     const int tiles_x = (g.nx + TX - 1) / TX, tiles_y = (g.ny + TY - 1) / TY;
     const int tx = static_cast<int>(local % tiles_x);
     const unsigned long long rest = local / tiles_x;
     const int ty = static_cast<int>(rest % tiles_y);
     const int tz = static_cast<int>(rest / tiles_y);
-    const int vx = tx * TX + lx, vy = ty * TY + ly;
-    const float px = cell_center(g.ox, vx, g.voxel), py = cell_center(g.oy, vy, g.voxel);
-    float pz[VPL], best[VPL];
-    bool active[VPL];
+    vx = tx * TX + lane % TX;
+    vy = ty * TY + (lane / TX) % TY;
+    vz0 = tz * TZ + lane / kLayer;
+    px = cell_center(g.ox, vx, g.voxel);
+    py = cell_center(g.oy, vy, g.voxel);
 #pragma unroll
     for (int v = 0; v < VPL; ++v) {
-      const int vz = tz * TZ + lz + v * kLanesZ;
+      const int vz = vz0 + v * kLanesZ;
       active[v] = vx < g.nx && vy < g.ny && vz < g.nz;
       pz[v] = cell_center(g.oz, vz, g.voxel);
-      best[v] = active[v] ? __int_as_float(0x7f800000) : -1.0f;  // inactive cells never ask for work
     }
+  }
 
-    auto test_leaf = [&](int first, int count) {
-      if (first < 0 || count > num_tris - first) {
-        corrupt = true;
-        return;
-      }
-      for (int k = 0; k < count; ++k) {
-        const TriRec *tr = tris + first + k;
-        const float4 r0 = __ldg(&tr->r0), r1 = __ldg(&tr->r1), r2 = __ldg(&tr->r2), r3 = __ldg(&tr->r3);
+  __device__ __forceinline__ uint64_t cell(int v) const {
+    return (uint64_t(vz0 + v * kLanesZ) * g.ny + vy) * g.nx + vx;
+  }
+};
+
+template <int VPL, bool COUNT>
+__device__ __forceinline__ void test_leaf(const TriRec *__restrict__ tris, int num_tris, int first, int count,
+                                          float px, float py, const float (&pz)[VPL], float (&best)[VPL],
+                                          WalkStats &ws) {
+  if (first < 0 || count > num_tris - first) {
+    ws.corrupt = true;
+    return;
+  }
+  for (int k = 0; k < count; ++k) {
+    const TriRec *tr = tris + first + k;
+    const float4 r0 = __ldg(&tr->r0), r3 = __ldg(&tr->r3);
+    // The squared distance to the triangle's plane, (ap . n)^2 / |n|^2, bounds the squared
+    // distance to the triangle from below: skip the triangle when no cell could improve.
+    bool need = false;
 #pragma unroll
-        for (int v = 0; v < VPL; ++v) best[v] = fminf(best[v], point_tri_dist2(px, py, pz[v], r0, r1, r2, r3));
-      }
-      if (COUNT) tri_tests += static_cast<unsigned long long>(count) * kWarp * VPL;
-    };
+    for (int v = 0; v < VPL; ++v) {
+      const float h = (px - r0.x) * r3.x + (py - r0.y) * r3.y + (pz[v] - r0.z) * r3.z;
+      need |= h * h * r3.w < best[v];
+    }
+    if (COUNT) ws.plane_tests += kWarp * VPL;
+    if (!__any_sync(kFull, need)) continue;
+    const float4 r1 = __ldg(&tr->r1), r2 = __ldg(&tr->r2);
+#pragma unroll
+    for (int v = 0; v < VPL; ++v) best[v] = fminf(best[v], point_tri_dist2(px, py, pz[v], r0, r1, r2, r3));
+    if (COUNT) ws.tri_tests += kWarp * VPL;
+  }
+}
 
-    int cur = M.root, sp = 0, stk0 = 0, stk1 = 0;
-    for (long long steps = 0;; ++steps) {
-      if (steps > step_limit || cur >= num_nodes) {
-        corrupt = true;
-        break;
+// When a walk may stop early: every `every` steps it reads the pass's tile counter, and it stops
+// once every tile has been handed out (the pass is in its tail, where a long walk would run
+// alone). every = 0: never.
+struct TailCheck {
+  const unsigned long long *counter;
+  unsigned long long total;
+  int every;
+};
+
+// Walks the subtree below inner node `start` for this lane's cells, tightening best[] (squared
+// distances; inactive cells hold -1 and never ask for work). Returns false when the walk stopped
+// early by the tail check with work left (best[] then holds upper bounds); a walk past the limit a
+// correct tree allows stops with the corrupt flag.
+template <int VPL, int STACK, bool COUNT>
+__device__ __forceinline__ bool walk(const Node *__restrict__ nodes, const TriRec *__restrict__ tris, int num_nodes,
+                                     int num_tris, int start, TailCheck tail, int lane, float px, float py,
+                                     const float (&pz)[VPL], const bool (&active)[VPL], float (&best)[VPL],
+                                     WalkStats &ws) {
+  static_assert(STACK == 32 || STACK == 64, "stack depth is one or two registers per lane");
+  // A correct tree expands each inner node at most once per walk and pops at most once per push.
+  const int step_limit = num_nodes > (INT_MAX - 64) / 2 ? INT_MAX - 1 : 2 * num_nodes + 64;
+  int next_check = tail.every > 0 ? tail.every : INT_MAX;
+  int cur = start, sp = 0, stk0 = 0, stk1 = 0;
+  for (int steps = 0;; ++steps) {
+    if (steps > step_limit || cur >= num_nodes) {
+      ws.corrupt = true;
+      return true;
+    }
+    if (steps >= next_check) {
+      unsigned long long handed = 0;
+      if (lane == 0) handed = *reinterpret_cast<const volatile unsigned long long *>(tail.counter);
+      handed = __shfl_sync(kFull, handed, 0);
+      if (handed >= tail.total) return false;
+      next_check = steps + tail.every;
+    }
+    if (cur < 0) {
+      if (sp == 0) return true;
+      --sp;
+      const int e = __shfl_sync(kFull, (STACK == 32 || sp < 32) ? stk0 : stk1, sp & 31);
+      if ((e >> 1) >= num_nodes) {
+        ws.corrupt = true;
+        return true;
       }
-      if (cur < 0) {
-        if (sp == 0) break;
-        --sp;
-        const int e = __shfl_sync(kFull, (STACK == 32 || sp < 32) ? stk0 : stk1, sp & 31);
-        if ((e >> 1) >= num_nodes) {
-          corrupt = true;
+      const Node *np = nodes + (e >> 1);
+      const float4 n0 = __ldg(&np->n0), n1 = __ldg(&np->n1), n2 = __ldg(&np->n2);
+      const int4 n3 = __ldg(&np->n3);
+      float lx0, ly0, lz0, hx0, hy0, hz0;
+      int ref, cnt;
+      if (e & 1) {
+        lx0 = n1.z; ly0 = n1.w; lz0 = n2.x; hx0 = n2.y; hy0 = n2.z; hz0 = n2.w;
+        ref = n3.y; cnt = n3.w;
+      } else {
+        lx0 = n0.x; ly0 = n0.y; lz0 = n0.z; hx0 = n0.w; hy0 = n1.x; hz0 = n1.y;
+        ref = n3.x; cnt = n3.z;
+      }
+      bool want = false;
+#pragma unroll
+      for (int v = 0; v < VPL; ++v) want |= box_dist2(px, py, pz[v], lx0, ly0, lz0, hx0, hy0, hz0) < best[v];
+      if (COUNT) ws.box_tests += kWarp * VPL;
+      if (!__any_sync(kFull, want)) continue;
+      if (cnt > 0) test_leaf<VPL, COUNT>(tris, num_tris, ref, cnt, px, py, pz, best, ws);
+      else cur = ref;
+      continue;
+    }
+    const int node = cur;
+    const Node *np = nodes + node;
+    const float4 n0 = __ldg(&np->n0), n1 = __ldg(&np->n1), n2 = __ldg(&np->n2);
+    const int4 n3 = __ldg(&np->n3);
+    float d0[VPL], d1[VPL];
+    float m0 = kInf, m1 = kInf;
+    bool w0 = false, w1 = false;
+#pragma unroll
+    for (int v = 0; v < VPL; ++v) {
+      d0[v] = box_dist2(px, py, pz[v], n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
+      d1[v] = box_dist2(px, py, pz[v], n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
+      w0 |= d0[v] < best[v];
+      w1 |= d1[v] < best[v];
+      if (active[v]) {
+        m0 = fminf(m0, d0[v]);
+        m1 = fminf(m1, d1[v]);
+      }
+    }
+    if (COUNT) ws.box_tests += 2 * kWarp * VPL;
+    w0 = __any_sync(kFull, w0) && n3.z >= 0;
+    w1 = __any_sync(kFull, w1) && n3.w >= 0;
+    const bool second_first =
+        __reduce_min_sync(kFull, __float_as_uint(m1)) < __reduce_min_sync(kFull, __float_as_uint(m0));
+    const int near_ref = second_first ? n3.y : n3.x, near_cnt = second_first ? n3.w : n3.z;
+    const int far_ref = second_first ? n3.x : n3.y, far_cnt = second_first ? n3.z : n3.w;
+    bool near_w = second_first ? w1 : w0, far_w = second_first ? w0 : w1;
+    cur = -1;
+    if (near_w) {
+      if (near_cnt > 0) {
+        test_leaf<VPL, COUNT>(tris, num_tris, near_ref, near_cnt, px, py, pz, best, ws);
+        if (far_w) {
+          bool w = false;
+#pragma unroll
+          for (int v = 0; v < VPL; ++v) w |= (second_first ? d0[v] : d1[v]) < best[v];
+          far_w = __any_sync(kFull, w);
+        }
+      } else {
+        cur = near_ref;
+      }
+    }
+    if (far_w) {
+      if (cur >= 0) {
+        if (sp < STACK) {
+          const int e = (node << 1) | (second_first ? 0 : 1);
+          if (STACK == 32 || sp < 32) {
+            if (lane == sp) stk0 = e;
+          } else if (lane == sp - 32) {
+            stk1 = e;
+          }
+          ++sp;
+        } else {
+          ws.overflow = true;
+        }
+      } else if (far_cnt > 0) {
+        test_leaf<VPL, COUNT>(tris, num_tris, far_ref, far_cnt, px, py, pz, best, ws);
+      } else {
+        cur = far_ref;
+      }
+    }
+  }
+}
+
+// Signs (parity) and writes a tile's distances.
+template <int TX, int TY, int TZ>
+__device__ __forceinline__ void store_cells(const DistanceArgs &a, const TileCells<TX, TY, TZ> &c,
+                                            const float (&best)[TileCells<TX, TY, TZ>::VPL]) {
+  constexpr int VPL = TileCells<TX, TY, TZ>::VPL;
+  const MeshRec &M = *c.M;
+  int inside[VPL];
+#pragma unroll
+  for (int v = 0; v < VPL; ++v) inside[v] = 0;
+  if (M.sign == kSignParity && c.vx < c.g.nx && c.vy < c.g.ny) {
+    const uint64_t col = M.col_base + uint64_t(c.vy) * c.g.nx + c.vx;
+    const uint64_t s0 = __ldg(a.col_start + col), s1 = __ldg(a.col_start + col + 1);
+    for (uint64_t k = s0; k < s1; ++k) {
+      const float zc = __ldg(a.col_z + k);
+#pragma unroll
+      for (int v = 0; v < VPL; ++v) inside[v] ^= zc > c.pz[v] ? 1 : 0;
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < VPL; ++v) {
+    if (!c.active[v]) continue;
+    const float d = sqrtf(best[v]);
+    M.dist[c.cell(v)] = inside[v] ? -d : d;
+  }
+}
+
+template <bool COUNT>
+__device__ __forceinline__ void flush_stats(const DistanceArgs &a, const WalkStats &ws, int lane) {
+  if (ws.overflow) atomic_or_err(a.err, kErrStackOverflow);
+  if (ws.corrupt) atomic_or_err(a.err, kErrCorruptTree);
+  if (COUNT && a.work_counters && lane == 0) {
+    atomicAdd(a.work_counters, ws.box_tests);
+    atomicAdd(a.work_counters + 1, ws.tri_tests);
+    atomicAdd(a.work_counters + 3, ws.plane_tests);
+  }
+}
+
+// Pass A: one warp per tile, tiles from a global counter; tiles over the step budget are deferred.
+template <int TX, int TY, int TZ, int STACK, bool COUNT>
+__global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a) {
+  using Cells = TileCells<TX, TY, TZ>;
+  constexpr int VPL = Cells::VPL;
+  const int lane = threadIdx.x & 31;
+  const BatchDev &B = a.batch;
+  WalkStats ws;
+  TailCheck tail{a.tile_counter, B.total_tiles,
+                 (a.defer_list && a.step_budget > 0) ? static_cast<int>(min(a.step_budget, 1ll << 30)) : 0};
+  const TailCheck never{nullptr, 0, 0};
+
+  for (;;) {
+    unsigned long long tile = 0;
+    if (lane == 0) tile = atomicAdd(a.tile_counter, 1ull);
+    tile = __shfl_sync(kFull, tile, 0);
+    if (tile >= B.total_tiles) break;
+    Cells c;
+    c.locate(B, tile, lane);
+    const MeshRec &M = *c.M;
+    float best[VPL];
+#pragma unroll
+    for (int v = 0; v < VPL; ++v) best[v] = c.active[v] ? kInf : -1.0f;
+    bool done = walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, M.root, tail, lane, c.px, c.py,
+                                        c.pz, c.active, best, ws);
+    if (!done) {
+      unsigned long long slot = 0;
+      if (lane == 0) slot = atomicAdd(a.defer_counters, 1ull);
+      slot = __shfl_sync(kFull, slot, 0);
+      if (slot < a.defer_capacity) {
+        if (lane == 0) a.defer_list[slot] = tile;
+#pragma unroll
+        for (int v = 0; v < VPL; ++v)
+          if (c.active[v]) M.dist[c.cell(v)] = best[v];  // the bounds pass B starts from
+        continue;
+      }
+      // The list is full: finish the tile here, from the bounds found so far.
+      walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, M.root, never, lane, c.px, c.py, c.pz,
+                              c.active, best, ws);
+    }
+    store_cells<TX, TY, TZ>(a, c, best);
+  }
+  flush_stats<COUNT>(a, ws, lane);
+}
+
+// Pass B: one block per deferred tile; its warps share the tile's subtrees and bounds.
+template <int TX, int TY, int TZ, int STACK, bool COUNT>
+__global__ __launch_bounds__(kThreads) void k_distance_deferred(DistanceArgs a) {
+  using Cells = TileCells<TX, TY, TZ>;
+  constexpr int VPL = Cells::VPL;
+  constexpr int kItems = 1 << kSplitBits;
+  __shared__ unsigned long long s_tile;
+  __shared__ int s_item;
+  __shared__ uint32_t s_best[VPL * kWarp];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const BatchDev &B = a.batch;
+  WalkStats ws;
+  const unsigned long long count = a.defer_counters[0];
+  const unsigned long long total = count < a.defer_capacity ? count : a.defer_capacity;
+
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const unsigned long long k = atomicAdd(a.defer_counters + 1, 1ull);
+      s_tile = k < total ? a.defer_list[k] : ~0ull;
+      s_item = 0;
+    }
+    __syncthreads();
+    const unsigned long long tile = s_tile;
+    if (tile == ~0ull) break;
+    Cells c;
+    c.locate(B, tile, lane);
+    const MeshRec &M = *c.M;
+    float best[VPL];
+#pragma unroll
+    for (int v = 0; v < VPL; ++v) {
+      best[v] = c.active[v] ? M.dist[c.cell(v)] : -1.0f;
+      if (warp == 0) s_best[v * kWarp + lane] = __float_as_uint(c.active[v] ? best[v] : 0.0f);
+    }
+    __syncthreads();
+    for (;;) {
+      int item = 0;
+      if (lane == 0) item = atomicAdd(&s_item, 1);
+      item = __shfl_sync(kFull, item, 0);
+      if (item >= kItems) break;
+#pragma unroll
+      for (int v = 0; v < VPL; ++v)
+        if (c.active[v]) best[v] = fminf(best[v], __uint_as_float(s_best[v * kWarp + lane]));
+      // Descend to this item's subtree: each node with two children consumes one bit of the item
+      // (most significant first); a leaf reached early is tested by the item whose remaining bits
+      // are all zero.
+      int cur = M.root, bits = kSplitBits;
+      bool walk_it = false;
+      for (int guard = 0; guard < 64; ++guard) {
+        if (bits == 0) {
+          walk_it = true;
           break;
         }
-        const Node *np = nodes + (e >> 1);
+        if (cur < 0 || cur >= M.bvh_nodes) {
+          ws.corrupt = true;
+          break;
+        }
+        const Node *np = M.nodes + cur;
         const float4 n0 = __ldg(&np->n0), n1 = __ldg(&np->n1), n2 = __ldg(&np->n2);
         const int4 n3 = __ldg(&np->n3);
-        float lx0, ly0, lz0, hx0, hy0, hz0;
-        int ref, cnt;
-        if (e & 1) {
-          lx0 = n1.z; ly0 = n1.w; lz0 = n2.x; hx0 = n2.y; hy0 = n2.z; hz0 = n2.w;
-          ref = n3.y; cnt = n3.w;
+        const bool e0 = n3.z < 0, e1 = n3.w < 0;
+        if (e0 && e1) break;
+        int which;
+        if (!e0 && !e1) {
+          --bits;
+          which = (item >> bits) & 1;
         } else {
-          lx0 = n0.x; ly0 = n0.y; lz0 = n0.z; hx0 = n0.w; hy0 = n1.x; hz0 = n1.y;
-          ref = n3.x; cnt = n3.z;
+          which = e0 ? 1 : 0;
         }
         bool want = false;
 #pragma unroll
-        for (int v = 0; v < VPL; ++v) want |= box_dist2(px, py, pz[v], lx0, ly0, lz0, hx0, hy0, hz0) < best[v];
-        if (COUNT) box_tests += kWarp * VPL;
-        if (!__any_sync(kFull, want)) continue;
-        if (cnt > 0) test_leaf(ref, cnt);
-        else cur = ref;
-        continue;
+        for (int v = 0; v < VPL; ++v) {
+          const float d = which ? box_dist2(c.px, c.py, c.pz[v], n1.z, n1.w, n2.x, n2.y, n2.z, n2.w)
+                                : box_dist2(c.px, c.py, c.pz[v], n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
+          want |= d < best[v];
+        }
+        if (COUNT) ws.box_tests += kWarp * VPL;
+        if (!__any_sync(kFull, want)) break;
+        const int ref = which ? n3.y : n3.x, cnt = which ? n3.w : n3.z;
+        if (cnt > 0) {
+          if ((item & ((1 << bits) - 1)) == 0)
+            test_leaf<VPL, COUNT>(M.tris, M.bvh_tris, ref, cnt, c.px, c.py, c.pz, best, ws);
+          break;
+        }
+        cur = ref;
       }
-      const int node = cur;
-      const Node *np = nodes + node;
-      const float4 n0 = __ldg(&np->n0), n1 = __ldg(&np->n1), n2 = __ldg(&np->n2);
-      const int4 n3 = __ldg(&np->n3);
-      float d0[VPL], d1[VPL];
-      float m0 = __int_as_float(0x7f800000), m1 = m0;
-      bool w0 = false, w1 = false;
+      if (walk_it)
+        walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, cur, TailCheck{nullptr, 0, 0}, lane, c.px,
+                                c.py, c.pz, c.active, best, ws);
 #pragma unroll
-      for (int v = 0; v < VPL; ++v) {
-        d0[v] = box_dist2(px, py, pz[v], n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
-        d1[v] = box_dist2(px, py, pz[v], n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
-        w0 |= d0[v] < best[v];
-        w1 |= d1[v] < best[v];
-        if (active[v]) {
-          m0 = fminf(m0, d0[v]);
-          m1 = fminf(m1, d1[v]);
-        }
-      }
-      if (COUNT) box_tests += 2 * kWarp * VPL;
-      w0 = __any_sync(kFull, w0) && n3.z >= 0;
-      w1 = __any_sync(kFull, w1) && n3.w >= 0;
-      const bool second_first =
-          __reduce_min_sync(kFull, __float_as_uint(m1)) < __reduce_min_sync(kFull, __float_as_uint(m0));
-      const int near_ref = second_first ? n3.y : n3.x, near_cnt = second_first ? n3.w : n3.z;
-      const int far_ref = second_first ? n3.x : n3.y, far_cnt = second_first ? n3.z : n3.w;
-      bool near_w = second_first ? w1 : w0, far_w = second_first ? w0 : w1;
-      cur = -1;
-      if (near_w) {
-        if (near_cnt > 0) {
-          test_leaf(near_ref, near_cnt);
-          if (far_w) {
-            bool w = false;
-#pragma unroll
-            for (int v = 0; v < VPL; ++v) w |= (second_first ? d0[v] : d1[v]) < best[v];
-            far_w = __any_sync(kFull, w);
-          }
-        } else {
-          cur = near_ref;
-        }
-      }
-      if (far_w) {
-        if (cur >= 0) {
-          if (sp < STACK) {
-            const int e = (node << 1) | (second_first ? 0 : 1);
-            if (STACK == 32 || sp < 32) {
-              if (lane == sp) stk0 = e;
-            } else if (lane == sp - 32) {
-              stk1 = e;
-            }
-            ++sp;
-          } else {
-            overflow = true;
-          }
-        } else if (far_cnt > 0) {
-          test_leaf(far_ref, far_cnt);
-        } else {
-          cur = far_ref;
-        }
-      }
+      for (int v = 0; v < VPL; ++v)
+        if (c.active[v]) atomicMin(&s_best[v * kWarp + lane], __float_as_uint(best[v]));
     }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+      for (int v = 0; v < VPL; ++v) best[v] = c.active[v] ? __uint_as_float(s_best[v * kWarp + lane]) : -1.0f;
+      store_cells<TX, TY, TZ>(a, c, best);
+    }
+    __syncthreads();
+  }
+  flush_stats<COUNT>(a, ws, lane);
+}
 
-    // Sign and store.
-    int inside[VPL];
-#pragma unroll
-    for (int v = 0; v < VPL; ++v) inside[v] = 0;
-    if (M.sign == kSignParity && vx < g.nx && vy < g.ny) {
-      const uint64_t col = M.col_base + uint64_t(vy) * g.nx + vx;
-      const uint64_t s0 = __ldg(a.col_start + col), s1 = __ldg(a.col_start + col + 1);
-      for (uint64_t k = s0; k < s1; ++k) {
-        const float zc = __ldg(a.col_z + k);
-#pragma unroll
-        for (int v = 0; v < VPL; ++v) inside[v] ^= zc > pz[v] ? 1 : 0;
-      }
-    }
-#pragma unroll
-    for (int v = 0; v < VPL; ++v) {
-      if (!active[v]) continue;
-      const int vz = tz * TZ + lz + v * kLanesZ;
-      const uint64_t cell = (uint64_t(vz) * g.ny + vy) * g.nx + vx;
-      const float d = sqrtf(best[v]);
-      M.dist[cell] = inside[v] ? -d : d;
-    }
-  }
-  if (overflow) atomic_or_err(a.err, kErrStackOverflow);
-  if (corrupt) atomic_or_err(a.err, kErrCorruptTree);
-  if (COUNT && a.work_counters && lane == 0) {
-    atomicAdd(a.work_counters, box_tests);
-    atomicAdd(a.work_counters + 1, tri_tests);
-  }
+template <typename K>
+int blocks_per_sm(K kernel) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0);
+  return per_sm > 0 ? per_sm : 1;
 }
 
 template <int I, int STACK, bool COUNT>
 cudaError_t launch_shape(const DistanceArgs &a, int num_sms, cudaStream_t st) {
   constexpr Shape s = kShapes[I];
-  static int per_sm = 0;
-  if (per_sm == 0) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_distance<s.tx, s.ty, s.tz, STACK, COUNT>, kThreads, 0);
-    if (per_sm <= 0) per_sm = 1;
-  }
+  static const int per_sm = blocks_per_sm(k_distance<s.tx, s.ty, s.tz, STACK, COUNT>);
+  static const int per_sm_b = blocks_per_sm(k_distance_deferred<s.tx, s.ty, s.tz, STACK, COUNT>);
   const unsigned long long warps_needed = a.batch.total_tiles;
   unsigned long long blocks = static_cast<unsigned long long>(num_sms) * per_sm;
-  blocks = std::min<unsigned long long>(blocks, (warps_needed + (kThreads / kWarp) - 1) / (kThreads / kWarp));
+  blocks = std::min<unsigned long long>(blocks, (warps_needed + kWarpsPerBlock - 1) / kWarpsPerBlock);
   if (blocks < 1) blocks = 1;
   cudaError_t e = cudaMemsetAsync(a.tile_counter, 0, sizeof(unsigned long long), st);
+  if (e == cudaSuccess && a.defer_list) e = cudaMemsetAsync(a.defer_counters, 0, 2 * sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   k_distance<s.tx, s.ty, s.tz, STACK, COUNT><<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(a);
+  note_launch();
+  e = cudaGetLastError();
+  if (e != cudaSuccess || !a.defer_list || a.step_budget <= 0) return e;
+  // Pass B: a persistent grid; the number of deferred tiles is read on the device.
+  const unsigned long long blocks_b =
+      std::min<unsigned long long>(static_cast<unsigned long long>(num_sms) * per_sm_b, a.defer_capacity);
+  k_distance_deferred<s.tx, s.ty, s.tz, STACK, COUNT>
+      <<<static_cast<unsigned>(std::max<unsigned long long>(blocks_b, 1)), kThreads, 0, st>>>(a);
   note_launch();
   return cudaGetLastError();
 }
@@ -261,6 +490,10 @@ uint64_t tiles_for(const GridDev &g, int id) {
   int tx, ty, tz;
   tile_shape(id, tx, ty, tz);
   return uint64_t((g.nx + tx - 1) / tx) * uint64_t((g.ny + ty - 1) / ty) * uint64_t((g.nz + tz - 1) / tz);
+}
+
+uint64_t defer_capacity_for(uint64_t total_tiles) {
+  return std::min<uint64_t>(total_tiles, std::max<uint64_t>(4096, total_tiles / 8));
 }
 
 cudaError_t distance_launch(const DistanceArgs &a, int tile_id, int stack_depth, int num_sms, cudaStream_t st) {

@@ -201,4 +201,11 @@ size_t boundary_caps(const float *verts, uint32_t V, const uint32_t *idx, uint32
   return loops;
 }
 
+void srgb_to_linear_table(float out[256]) {
+  for (int b = 0; b < 256; ++b) {
+    const float c = static_cast<float>(b) / 255.0f;
+    out[b] = c <= 0.04045f ? c / 12.92f : std::pow((c + 0.055f) / 1.055f, 2.4f);
+  }
+}
+
 }  // namespace sdfb

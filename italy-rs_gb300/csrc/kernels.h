@@ -144,7 +144,16 @@ struct DistanceArgs {
   const float *col_z;
   uint32_t *err;
   unsigned long long *tile_counter;   // zeroed by the launcher
-  unsigned long long *work_counters;  // optional: [0] box tests, [1] triangle tests (lanes)
+  unsigned long long *work_counters;  // optional: [0] box, [1] triangle, [3] plane tests (lanes)
+  // Deferral of long tiles (none when defer_list is null or step_budget <= 0): every step_budget
+  // traversal steps a walk checks whether all tiles have been handed out and, if so, defers its
+  // tile. The list holds defer_capacity tile indices; defer_counters[0] counts deferred tiles (it
+  // may pass the capacity), [1] is the second pass's tile counter. Both counters are zeroed by the
+  // launcher.
+  unsigned long long *defer_list;
+  unsigned long long defer_capacity;
+  unsigned long long *defer_counters;
+  long long step_budget;
 };
 
 int tile_shape_count();
@@ -152,7 +161,32 @@ int tile_shape_count();
 void tile_shape(int id, int &tx, int &ty, int &tz);
 uint64_t tiles_for(const GridDev &g, int tile_id);
 // stack_depth: 32 or 64 entries (32 keeps the stack in one register per lane).
+// Deferred-list capacity for a launch of total_tiles tiles.
+uint64_t defer_capacity_for(uint64_t total_tiles);
 cudaError_t distance_launch(const DistanceArgs &a, int tile_id, int stack_depth, int num_sms, cudaStream_t st);
+
+// Every (cell, triangle) pair of a ONE-mesh batch that passes the occupancy rule, as keys
+// (cell << tri_bits) | local triangle, appended in no particular order (the mesh's occupancy grid
+// is written as well). *hit_count (device) receives the number of hits, also when it exceeds
+// `capacity` (then only `capacity` keys are written).
+cudaError_t occupancy_hits(const BatchDev &B, void *temp, size_t temp_bytes, uint64_t *keys, uint64_t capacity,
+                           unsigned long long *hit_count, int tri_bits, int num_sms, cudaStream_t st);
+
+// ---- weld.cu ----------------------------------------------------------------------------------
+// weldPositions on the device: welded[i] = the first-occurrence number of position i's lattice key
+// (cell: the weld lattice, weld_cell in host_mesh.h); first_of (optional, num_unique entries) gets
+// each number's first position. Synchronises the stream (*num_unique is host memory).
+size_t weld_temp_bytes(uint64_t n);
+cudaError_t weld_device(const float *pos, uint64_t n, float cell, uint32_t *welded, uint32_t *first_of, void *temp,
+                        size_t temp_bytes, uint32_t *num_unique, int num_sms, cudaStream_t st);
+// out[u] = pos[first_of[u]] (3 floats) for u < U.
+cudaError_t gather_unique(const float *pos, const uint32_t *first_of, uint64_t U, float *out, int num_sms,
+                          cudaStream_t st);
+// Edge census of a welded triangle list (degenerate triangles skipped); every index must be below
+// num_unique (0: unknown). Synchronises the stream.
+size_t watertight_temp_bytes(uint64_t T);
+cudaError_t watertight_device(const uint32_t *welded, uint64_t T, uint32_t num_unique, void *temp, size_t temp_bytes,
+                              uint64_t *boundary, uint64_t *nonmanifold, int num_sms, cudaStream_t st);
 
 // ---- sparse.cu --------------------------------------------------------------------------------
 size_t sparse_temp_bytes(size_t cells, size_t max_out);

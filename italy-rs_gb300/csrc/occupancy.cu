@@ -88,10 +88,34 @@ __global__ __launch_bounds__(kThreads) void k_occ_clear(BatchDev B) {
   }
 }
 
-template <bool FIRST>
+// Appends of (cell, triangle) hits: a warp-aggregated atomic reserves the slots of the lanes that
+// hit together; keys past the capacity are counted but not written.
+struct HitSink {
+  uint64_t *keys = nullptr;
+  uint64_t capacity = 0;
+  unsigned long long *count = nullptr;
+  int tri_bits = 0;
+};
+
+__device__ __forceinline__ void append_hit(const HitSink &h, bool hit, uint64_t key) {
+  const unsigned mask = __activemask();
+  const unsigned ballot = __ballot_sync(mask, hit);
+  if (!ballot) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(ballot) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(h.count, static_cast<unsigned long long>(__popc(ballot)));
+  base = __shfl_sync(mask, base, leader);
+  if (hit) {
+    const unsigned long long pos = base + __popc(ballot & ((1u << lane) - 1u));
+    if (pos < h.capacity) h.keys[pos] = key;
+  }
+}
+
+template <bool FIRST, bool HITS>
 __global__ __launch_bounds__(kThreads) void k_occ_test(BatchDev B, const uint64_t *__restrict__ starts,
                                                        uint32_t *__restrict__ first_tri,
-                                                       unsigned long long *__restrict__ sat_tests) {
+                                                       unsigned long long *__restrict__ sat_tests, HitSink sink) {
   const uint64_t T = B.total_tris;
   const uint64_t total = starts[T];
   const uint64_t stride = uint64_t(gridDim.x) * kThreads * kExpandChunk;
@@ -117,11 +141,13 @@ __global__ __launch_bounds__(kThreads) void k_occ_test(BatchDev B, const uint64_
       const int z = tc.lo[2] + static_cast<int>(k / (uint64_t(sx) * sy));
       const f3 c = {cell_center(g.ox, x, g.voxel), cell_center(g.oy, y, g.voxel), cell_center(g.oz, z, g.voxel)};
       ++tests;
-      if (sat_overlap(c, __fmul_rn(g.voxel, 0.5f), tc.a, tc.b, tc.c)) {
-        const uint64_t cell = (uint64_t(z) * g.ny + y) * g.nx + x;
+      const bool hit = sat_overlap(c, __fmul_rn(g.voxel, 0.5f), tc.a, tc.b, tc.c);
+      const uint64_t cell = (uint64_t(z) * g.ny + y) * g.nx + x;
+      if (hit) {
         M.occ[cell] = 1;
         if (FIRST) atomicMin(first_tri + cell, static_cast<uint32_t>(t - B.tri_starts[tc.mesh]));
       }
+      if (HITS) append_hit(sink, hit, (cell << sink.tri_bits) | (t - B.tri_starts[tc.mesh]));
     }
   }
   if (sat_tests) {
@@ -178,9 +204,36 @@ cudaError_t occupancy_batch(const BatchDev &B, uint32_t *first_tri, void *temp, 
   note_launch();
   if ((e = exclusive_scan_u32(o.items, o.starts, T, Scratch{o.scratch, o.scratch_bytes}, st)) != cudaSuccess) return e;
   if (first_tri)
-    k_occ_test<true><<<num_sms * 8, kThreads, 0, st>>>(B, o.starts, first_tri, sat_tests);
+    k_occ_test<true, false><<<num_sms * 8, kThreads, 0, st>>>(B, o.starts, first_tri, sat_tests, HitSink());
   else
-    k_occ_test<false><<<num_sms * 8, kThreads, 0, st>>>(B, o.starts, nullptr, sat_tests);
+    k_occ_test<false, false><<<num_sms * 8, kThreads, 0, st>>>(B, o.starts, nullptr, sat_tests, HitSink());
+  note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t occupancy_hits(const BatchDev &B, void *temp, size_t temp_bytes, uint64_t *keys, uint64_t capacity,
+                           unsigned long long *hit_count, int tri_bits, int num_sms, cudaStream_t st) {
+  if (B.num_meshes != 1) return cudaErrorInvalidValue;
+  const uint64_t T = B.total_tris;
+  cudaError_t e = cudaMemsetAsync(hit_count, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  if (B.total_cells) {
+    const uint64_t blocks = std::min<uint64_t>((B.total_cells + kThreads * 16 - 1) / (kThreads * 16), uint64_t(num_sms) * 16);
+    k_occ_clear<<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(B);
+    note_launch();
+  }
+  if (T == 0) return cudaGetLastError();
+  OccTemp o;
+  if (occ_layout(T, static_cast<char *>(temp), &o) > temp_bytes) return cudaErrorMemoryAllocation;
+  k_occ_items<<<static_cast<unsigned>((T + kThreads - 1) / kThreads), kThreads, 0, st>>>(B, o.items);
+  note_launch();
+  if ((e = exclusive_scan_u32(o.items, o.starts, T, Scratch{o.scratch, o.scratch_bytes}, st)) != cudaSuccess) return e;
+  HitSink sink;
+  sink.keys = keys;
+  sink.capacity = capacity;
+  sink.count = hit_count;
+  sink.tri_bits = tri_bits;
+  k_occ_test<false, true><<<num_sms * 8, kThreads, 0, st>>>(B, o.starts, nullptr, nullptr, sink);
   note_launch();
   return cudaGetLastError();
 }

@@ -41,10 +41,10 @@ using namespace sdfb;
   } while (0)
 
 // ---------------------------------------------------------------------------------------------
-// Tuned defaults: leaf size, tile shape and stack depth per (log2 triangles, log2 grid edge - 4).
-// The table is written by the autotuner (italy-rs_gb300/sdfb/autotune.py) as lines
-// "tri_bucket grid_bucket leaf tile stack" in italy-rs_gb300/tuning/gb300.tsv next to lib/;
-// SDFB_TUNING names another file.
+// Tuned defaults: leaf size, tile shape, stack depth and the distance pass's deferral budget per
+// (log2 triangles, log2 grid edge - 4). The table is written by the autotuner
+// (italy-rs_gb300/sdfb/autotune.py) as lines "tri_bucket grid_bucket leaf tile stack [budget]" in
+// italy-rs_gb300/tuning/gb300.tsv next to lib/; SDFB_TUNING names another file.
 
 int bucket_tris(uint64_t T) {
   int b = 0;
@@ -65,6 +65,7 @@ void load_tuning(sdfb_ctx *ctx) {
       ctx->tuned_leaf[i][j] = 4;
       ctx->tuned_tile[i][j] = 2;
       ctx->tuned_stack[i][j] = 64;
+      ctx->tuned_budget[i][j] = kDefaultStepBudget;
     }
   std::string path;
   if (const char *env = std::getenv("SDFB_TUNING")) {
@@ -81,12 +82,14 @@ void load_tuning(sdfb_ctx *ctx) {
   if (!f) return;
   char line[256];
   while (std::fgets(line, sizeof line, f)) {
-    int tb, nb, leaf, tile, stack;
-    if (line[0] == '#' || std::sscanf(line, "%d %d %d %d %d", &tb, &nb, &leaf, &tile, &stack) != 5) continue;
+    int tb, nb, leaf, tile, stack, budget = -1;
+    if (line[0] == '#' || std::sscanf(line, "%d %d %d %d %d %d", &tb, &nb, &leaf, &tile, &stack, &budget) < 5)
+      continue;
     if (tb < 0 || tb >= 32 || nb < 0 || nb >= 8) continue;
     if (leaf >= 1 && leaf <= 16) ctx->tuned_leaf[tb][nb] = leaf;
     if (tile >= 0 && tile < tile_shape_count()) ctx->tuned_tile[tb][nb] = tile;
     if (stack == 32 || stack == 64) ctx->tuned_stack[tb][nb] = stack;
+    if (budget >= 0) ctx->tuned_budget[tb][nb] = budget;  // 0 turns deferral off
   }
   std::fclose(f);
 }
@@ -125,14 +128,14 @@ void Workspace::release() {
     graph_key.clear();
   }
   DevBuf *b[] = {&batch_buf, &bvh, &build_tmp, &par_tmp, &col_start, &col_z, &col_s, &caps_bvh, &caps_tmp, &misc,
-                 &gwn_tmp};
+                 &gwn_tmp, &defer};
   for (DevBuf *x : b) x->release();
   staging.release();
 }
 
 uint64_t Workspace::bytes() const {
   const DevBuf *b[] = {&batch_buf, &bvh, &build_tmp, &par_tmp, &col_start, &col_z, &col_s, &caps_bvh, &caps_tmp,
-                       &misc, &gwn_tmp};
+                       &misc, &gwn_tmp, &defer};
   uint64_t s = 0;
   for (const DevBuf *x : b) s += x->cap;
   return s;
@@ -150,6 +153,7 @@ struct Layout {
   std::vector<uint64_t> tri, ptri, tile, gtile, cell, cap_tri, cap_zero;
   uint64_t total_cols = 0, gwn_cells = 0, cap_total = 0;
   int tile_id = 2, stack = 64;
+  long long step_budget = 0;
   bool resident = false;
   size_t o_recs = 0, o_tri = 0, o_ptri = 0, o_tile = 0, o_gtile = 0, o_cell = 0, o_caprecs = 0, o_captri = 0,
          o_capzero = 0, bytes = 0;
@@ -166,6 +170,7 @@ void make_layout(sdfb_ctx *ctx, const std::vector<PlanMesh> &ms, const sdfb_opts
   const int tb = bucket_tris(ms[big].T), nb = bucket_grid(ms[big].grid);
   L.tile_id = (o.tile >= 1 && o.tile <= tile_shape_count()) ? o.tile - 1 : ctx->tuned_tile[tb][nb];
   L.stack = (o.stack_depth == 32 || o.stack_depth == 64) ? o.stack_depth : ctx->tuned_stack[tb][nb];
+  L.step_budget = o.step_budget > 0 ? o.step_budget : (o.step_budget < 0 ? 0 : ctx->tuned_budget[tb][nb]);
   L.resident = ms[0].bvh != nullptr;
   uint64_t T_total = 0;
   for (const auto &p : ms) T_total += p.T;
@@ -388,6 +393,8 @@ sdfb_status enqueue_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, std::ve
     ENSURE(ws.caps_tmp, lbvh_temp_bytes(L.cap_total, K));
   }
   if (S.any_gwn) ENSURE(ws.gwn_tmp, gwn_temp_bytes(L.gwn_cells));
+  const uint64_t defer_cap = L.step_budget > 0 ? defer_capacity_for(L.tile.back()) : 0;
+  if (defer_cap > 0) ENSURE(ws.defer, defer_cap * 8);
   BvhDev bvh, caps;
   if (build) lbvh_bind(bvh, ws.bvh.p, T, M, false);
   if (K > 0) lbvh_bind(caps, ws.caps_bvh.p, L.cap_total, K, true);
@@ -406,6 +413,10 @@ sdfb_status enqueue_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, std::ve
   da.err = d_err;
   da.tile_counter = d_tile;
   da.work_counters = o.count_work ? d_work : nullptr;
+  da.defer_list = defer_cap > 0 ? static_cast<unsigned long long *>(ws.defer.p) : nullptr;
+  da.defer_capacity = defer_cap;
+  da.defer_counters = reinterpret_cast<unsigned long long *>(static_cast<char *>(ws.misc.p) + kMiscDeferOffset);
+  da.step_budget = L.step_budget;
   GwnInput gi;
   gi.batch = B;
   gi.col_start = static_cast<const uint64_t *>(ws.col_start.p);
@@ -448,9 +459,10 @@ sdfb_status enqueue_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, std::ve
                              static_cast<const uint8_t *>(ws.staging.p) + L.bytes);
     const void *ptrs[] = {ws.batch_buf.p, ws.bvh.p,  ws.build_tmp.p, ws.par_tmp.p,  ws.col_start.p,
                           ws.col_z.p,     ws.col_s.p, ws.misc.p,      ws.staging.p,  ws.caps_bvh.p,
-                          ws.caps_tmp.p,  ws.gwn_tmp.p, static_cast<void *>(st)};
+                          ws.caps_tmp.p,  ws.gwn_tmp.p, ws.defer.p, static_cast<void *>(st)};
     const uint64_t extra[] = {uint64_t(L.tile_id), uint64_t(L.stack), S.capacity, L.bytes, ws.build_tmp.cap,
-                              ws.par_tmp.cap, ws.caps_tmp.cap, uint64_t(o.band_voxels * 1e6f)};
+                              ws.par_tmp.cap, ws.caps_tmp.cap, uint64_t(o.band_voxels * 1e6f),
+                              uint64_t(L.step_budget), defer_cap};
     key.insert(key.end(), reinterpret_cast<const uint8_t *>(ptrs), reinterpret_cast<const uint8_t *>(ptrs) + sizeof ptrs);
     key.insert(key.end(), reinterpret_cast<const uint8_t *>(extra),
                reinterpret_cast<const uint8_t *>(extra) + sizeof extra);
@@ -535,17 +547,20 @@ sdfb_status finish_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, const Ba
     sv.ms_distance = ms_d;
     sv.voxels = S.total_cells;
     sv.triangles = S.total_tris;
-    unsigned long long w[3] = {0, 0, 0};
+    unsigned long long w[4] = {0, 0, 0, 0};
     cudaMemcpy(w, d_work, sizeof w, cudaMemcpyDeviceToHost);
     sv.box_tests = w[0];
     sv.tri_tests = w[1];
     sv.sat_tests = w[2];
-    sv.flops_distance = double(w[0]) * kFlopsPointBox + double(w[1]) * kFlopsPointTri;
+    sv.plane_tests = w[3];
+    sv.flops_distance =
+        double(w[0]) * kFlopsPointBox + double(w[1]) * kFlopsPointTri + double(w[3]) * kFlopsPointPlane;
     if (S.any_cross)
       cudaMemcpy(&sv.crossings, static_cast<uint64_t *>(ws.col_start.p) + S.total_cols, 8, cudaMemcpyDeviceToHost);
     if (S.any_gwn) cudaMemcpy(&sv.gwn_fp64_cells, gwn_refine_counter(ws.gwn_tmp.p), 8, cudaMemcpyDeviceToHost);
     sv.kernel_launches = S.launched;
     sv.graph_replayed = S.graphed ? 1 : 0;
+    cudaMemcpy(&sv.tiles_deferred, static_cast<char *>(ws.misc.p) + kMiscDeferOffset, 8, cudaMemcpyDeviceToHost);
     cudaGetLastError();  // a failed statistics read does not fail the bake
     const size_t n = std::min<size_t>(stats->struct_size ? stats->struct_size : sizeof sv, sizeof sv);
     std::memcpy(stats, &sv, n);

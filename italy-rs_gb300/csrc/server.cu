@@ -161,6 +161,7 @@ std::unique_ptr<sdfb_ctx> make_private_ctx(int device, int num_sms, const sdfb_c
   std::memcpy(c->tuned_leaf, tuned->tuned_leaf, sizeof c->tuned_leaf);
   std::memcpy(c->tuned_tile, tuned->tuned_tile, sizeof c->tuned_tile);
   std::memcpy(c->tuned_stack, tuned->tuned_stack, sizeof c->tuned_stack);
+  std::memcpy(c->tuned_budget, tuned->tuned_budget, sizeof c->tuned_budget);
   return c;
 }
 
@@ -326,8 +327,20 @@ void sdfb_server::run() {
     // retire finished waves (their event has completed)
     for (auto &wp : waves) {
       Wave &w = *wp;
-      if (w.busy && cudaEventQuery(w.done) == cudaSuccess) retire_wave(w);
-      else cudaGetLastError();
+      if (!w.busy) continue;
+      const cudaError_t q = cudaEventQuery(w.done);
+      if (q == cudaSuccess) {
+        retire_wave(w);
+      } else if (q != cudaErrorNotReady) {
+        // the context has failed: complete the wave's requests with an error, do not wait
+        cudaGetLastError();
+        {
+          std::lock_guard<std::mutex> g(mu);
+          for (Request *r : w.reqs)
+            if (r->status < 0) r->status = SDFB_ERR_CUDA;
+        }
+        retire_wave(w);
+      }
     }
     Wave *free_slot = nullptr;
     {
@@ -457,6 +470,16 @@ sdfb_status sdfb_mesh_register(sdfb_server *srv, const float *verts, uint32_t nu
     }
   }
   std::lock_guard<std::mutex> rg(srv->reg_mu);  // one registration at a time
+  {
+    // Another thread may have registered the same mesh while this one waited for reg_mu; a
+    // second build would replace a Resident that queued requests still point to.
+    std::lock_guard<std::mutex> g(srv->mu);
+    auto it = srv->meshes.find(h);
+    if (it != srv->meshes.end()) {
+      it->second->last_use = ++srv->tick;
+      return SDFB_OK;
+    }
+  }
   cudaSetDevice(srv->device);
   auto r = std::make_unique<Resident>();
   r->id = h;
@@ -519,7 +542,7 @@ sdfb_status sdfb_mesh_register(sdfb_server *srv, const float *verts, uint32_t nu
   if (s != SDFB_OK) return undo(s, srv->reg->err);
   std::lock_guard<std::mutex> g(srv->mu);
   r->last_use = ++srv->tick;
-  srv->meshes[h] = std::move(r);
+  srv->meshes.emplace(h, std::move(r));  // registrations are serialised by reg_mu: h is new
   return SDFB_OK;
 }
 

@@ -52,7 +52,7 @@ class Opts(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("sign_mode", C.c_int32), ("band_voxels", C.c_float),
                 ("leaf_size", C.c_int32), ("tile", C.c_int32), ("no_occupancy", C.c_int32),
                 ("no_distance", C.c_int32), ("count_work", C.c_int32), ("stack_depth", C.c_int32),
-                ("reserved", C.c_int32 * 7)]
+                ("step_budget", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
 class Stats(C.Structure):
@@ -63,7 +63,8 @@ class Stats(C.Structure):
                 ("voxels", C.c_uint64), ("triangles", C.c_uint64), ("sat_tests", C.c_uint64),
                 ("crossings", C.c_uint64), ("box_tests", C.c_uint64), ("tri_tests", C.c_uint64),
                 ("flops_distance", C.c_double), ("kernel_launches", C.c_uint64), ("gwn_fp64_cells", C.c_uint64),
-                ("graph_replayed", C.c_uint64), ("reserved", C.c_uint64 * 2)]
+                ("graph_replayed", C.c_uint64), ("tiles_deferred", C.c_uint64),
+                ("plane_tests", C.c_uint64), ("reserved", C.c_uint64 * 2)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "struct_size")}
@@ -82,6 +83,53 @@ class RequestInfo(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("status", C.c_int32), ("t_submit_ms", C.c_double),
                 ("t_admit_ms", C.c_double), ("t_done_ms", C.c_double), ("voxels", C.c_uint64),
                 ("mesh_was_resident", C.c_int32), ("pad", C.c_int32)]
+
+
+class Texture(C.Structure):
+    _fields_ = [("rgba", C.c_void_p), ("width", C.c_int32), ("height", C.c_int32), ("srgb", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class Material(C.Structure):
+    _fields_ = [("base_color", C.c_float * 3), ("metallic", C.c_float), ("roughness", C.c_float),
+                ("base_color_texture", C.c_int32)]
+
+
+class Materials(C.Structure):
+    _fields_ = [("struct_size", C.c_uint32), ("num_materials", C.c_uint32), ("materials", C.c_void_p),
+                ("triangle_material", C.c_void_p), ("num_triangle_material", C.c_uint64), ("uvs", C.c_void_p),
+                ("num_uvs", C.c_uint64), ("textures", C.c_void_p), ("num_textures", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+def make_materials(m: dict):
+    """(Materials, keep-alive list) from {"mat_f": (M, 5) base colour rgb, metallic, roughness;
+    "mat_tex": (M,) texture index or -1; "tri_mat": per-triangle indices; "uvs": (3T, 2);
+    "textures": [(rgba uint8 (h, w, 4), srgb), ...]} (the layout meshgen.random_materials makes)."""
+    mf = np.ascontiguousarray(m["mat_f"], np.float32).reshape(-1, 5)
+    mt = np.ascontiguousarray(m["mat_tex"], np.int32).reshape(-1)
+    mats = (Material * len(mt))()
+    for i in range(len(mt)):
+        mats[i].base_color[:] = [float(x) for x in mf[i, :3]]
+        mats[i].metallic, mats[i].roughness, mats[i].base_color_texture = float(mf[i, 3]), float(mf[i, 4]), int(mt[i])
+    tri = np.ascontiguousarray(m.get("tri_mat", np.zeros(0)), np.uint32).reshape(-1)
+    uvs = np.ascontiguousarray(m.get("uvs", np.zeros((0, 2))), np.float32).reshape(-1, 2)
+    texs = [(np.ascontiguousarray(t[0], np.uint8), bool(t[1])) for t in m.get("textures", [])]
+    tarr = (Texture * max(len(texs), 1))()
+    for k, (px, srgb) in enumerate(texs):
+        tarr[k].rgba = px.ctypes.data
+        tarr[k].width, tarr[k].height, tarr[k].srgb = px.shape[1], px.shape[0], int(srgb)
+    out = Materials()
+    out.struct_size = C.sizeof(Materials)
+    out.num_materials = len(mt)
+    out.materials = C.cast(mats, C.c_void_p)
+    out.triangle_material = tri.ctypes.data if len(tri) else None
+    out.num_triangle_material = len(tri)
+    out.uvs = uvs.ctypes.data if len(uvs) else None
+    out.num_uvs = len(uvs)
+    out.textures = C.cast(tarr, C.c_void_p) if texs else None
+    out.num_textures = len(texs)
+    return out, [mats, tri, uvs, texs, tarr]
 
 
 _P = C.c_void_p
@@ -114,6 +162,13 @@ SIGNATURES = {
     "sdfb_submit": (_i32, [_P, _u64, C.POINTER(GridDesc), C.POINTER(Opts), _P, _P, C.POINTER(_u64)]),
     "sdfb_poll": (_i32, [_P, _u64, _i32, C.POINTER(_i32), C.POINTER(RequestInfo)]),
     "sdfb_server_last_error": (C.c_char_p, [_P]),
+    "sdfb_bake_materials": (_i32, [_P, _P, _u32, C.POINTER(GridDesc), C.POINTER(Materials), _P, _P, _P]),
+    "sdfb_voxelize_sparse_colors": (_i32, [_P, _P, _u32, _P, _P, _i32, C.POINTER(Materials), _P, _P, _u64,
+                                           C.POINTER(_u64), _P, C.POINTER(C.c_float)]),
+    "sdfb_weld_device": (_i32, [_P, _P, _u32, _P, _P, _P, C.POINTER(_u32), _P]),
+    "sdfb_is_watertight_device": (_i32, [_P, _P, _u32, C.POINTER(_i32), C.POINTER(_u64), C.POINTER(_u64), _P]),
+    "sdfb_sample_sdf": (_i32, [_P, C.POINTER(GridDesc), _P, _P, _u64, _P]),
+    "sdfb_trace_sdf": (_i32, [_P, C.POINTER(GridDesc), _P, _P, _u64, C.c_float, C.c_float, _P]),
     "sdfb_occupancy_noalloc": (_i32, [_P, _u32, _P, _u32, C.POINTER(GridDesc), _P, _P]),
 }
 
@@ -163,8 +218,9 @@ def make_grid(origin, voxel, n) -> GridDesc:
 
 def make_opts(sign_mode: int = SIGN_AUTO, band_voxels: float = 1.0, leaf_size: int = 0, tile: int = 0,
               no_occupancy: bool = False, no_distance: bool = False, count_work: bool = False,
-              stack_depth: int = 0) -> Opts:
-    """tile: shape 1..6 (0 = tuned); leaf_size 1..16 (0 = tuned); stack_depth 32 or 64 (0 = tuned)."""
+              stack_depth: int = 0, step_budget: int = 0) -> Opts:
+    """tile: shape 1..6 (0 = tuned); leaf_size 1..16 (0 = tuned); stack_depth 32 or 64 (0 = tuned);
+    step_budget: traversal steps before a distance tile is deferred (0 = tuned, -1 = never)."""
     o = Opts()
     o.struct_size = C.sizeof(Opts)
     o.sign_mode = sign_mode
@@ -175,6 +231,7 @@ def make_opts(sign_mode: int = SIGN_AUTO, band_voxels: float = 1.0, leaf_size: i
     o.no_distance = int(no_distance)
     o.count_work = int(count_work)
     o.stack_depth = stack_depth
+    o.step_budget = step_budget
     return o
 
 
@@ -285,6 +342,69 @@ class Context:
                                      _ptr(dist), _ptr(occ), C.byref(stats) if stats is not None else None)
         self._check(st)
         return g, dist, occ
+
+    def bake_materials(self, positions, grid: GridDesc, materials: dict):
+        """bakePerCellMaterial on the device: (base colour float32[nz, ny, nx, 3], metallic, roughness)."""
+        p = _f32(positions).reshape(-1, 9)
+        m, keep = make_materials(materials)
+        col = np.empty(grid.shape + (3,), np.float32)
+        met = np.empty(grid.shape, np.float32)
+        rou = np.empty(grid.shape, np.float32)
+        self._check(self.lib.sdfb_bake_materials(self.h, _ptr(p), len(p), C.byref(grid), C.byref(m), _ptr(col),
+                                                 _ptr(met), _ptr(rou)))
+        del keep
+        return col, met, rou
+
+    def voxelize_sparse_colors(self, positions, bmin, bmax, resolution: int, materials: dict):
+        """voxelizeMesh with colours: (cells int32[n, 3], colours float32[n, 3], origin, voxel)."""
+        p = _f32(positions).reshape(-1, 9)
+        m, keep = make_materials(materials)
+        cap = 1 << 16
+        while True:
+            cells = np.empty((cap, 3), np.int32)
+            cols = np.empty((cap, 3), np.float32)
+            cnt = _u64()
+            origin = np.empty(3, np.float32)
+            vox = C.c_float()
+            self._check(self.lib.sdfb_voxelize_sparse_colors(
+                self.h, _ptr(p), len(p), _ptr(_f32(bmin).reshape(3)), _ptr(_f32(bmax).reshape(3)), int(resolution),
+                C.byref(m), _ptr(cells), _ptr(cols), cap, C.byref(cnt), _ptr(origin), C.byref(vox)))
+            if cnt.value <= cap:
+                del keep
+                return cells[:cnt.value].copy(), cols[:cnt.value].copy(), origin, vox.value
+            cap = int(cnt.value)
+
+    def weld_device(self, d_positions: int, num_positions: int, bmin, bmax, d_welded_out: int, stream: int = 0) -> int:
+        """Device weld; returns the unique count (welded indices are written to d_welded_out)."""
+        u = _u32()
+        self._check(self.lib.sdfb_weld_device(self.h, C.c_void_p(d_positions), num_positions,
+                                              _ptr(_f32(bmin).reshape(3)), _ptr(_f32(bmax).reshape(3)),
+                                              C.c_void_p(d_welded_out), C.byref(u), C.c_void_p(stream)))
+        return u.value
+
+    def is_watertight_device(self, d_welded: int, num_tris: int, stream: int = 0):
+        """Device watertight census: (watertight, boundary edges, non-manifold edges)."""
+        w, b, m = _i32(), _u64(), _u64()
+        self._check(self.lib.sdfb_is_watertight_device(self.h, C.c_void_p(d_welded), num_tris, C.byref(w), C.byref(b),
+                                                       C.byref(m), C.c_void_p(stream)))
+        return bool(w.value), b.value, m.value
+
+    def sample_sdf(self, grid: GridDesc, dist, points) -> np.ndarray:
+        """The renderer's trilinear sample (sampleSdf) of a baked grid at points (n, 3)."""
+        d = _f32(dist).reshape(-1)
+        p = _f32(points).reshape(-1, 3)
+        out = np.empty(len(p), np.float32)
+        self._check(self.lib.sdfb_sample_sdf(self.h, C.byref(grid), _ptr(d), _ptr(p), len(p), _ptr(out)))
+        return out
+
+    def trace_sdf(self, grid: GridDesc, dist, rays, tmin: float = 0.0, tmax: float = 1e30) -> np.ndarray:
+        """The renderer's SDF intersection per ray (n, 6): hit distance or -1."""
+        d = _f32(dist).reshape(-1)
+        r = _f32(rays).reshape(-1, 6)
+        out = np.empty(len(r), np.float32)
+        self._check(self.lib.sdfb_trace_sdf(self.h, C.byref(grid), _ptr(d), _ptr(r), len(r), float(tmin),
+                                            float(tmax), _ptr(out)))
+        return out
 
     def voxelize_sparse(self, positions, bmin, bmax, resolution: int):
         p = _f32(positions).reshape(-1, 3)

@@ -7,12 +7,15 @@ Three parameters of the distance pass trade against each other with the mesh and
     4x4x8, 8x4x4 cells with 1, 1, 2, 2, 4, 4 cells per lane): bigger tiles share one traversal
     among more cells but visit the union of their candidates;
   * traversal stack depth (32 or 64 entries): the shallow stack needs fewer registers but a deep
-    tree overflows it (the bake then reruns that launch with 64).
+    tree overflows it (the bake then reruns that launch with 64);
+  * step budget (traversal steps before a tile is handed to the block-per-tile second pass, or
+    never): a small budget moves more tiles into the pass that splits a tile's walk over a block.
 
 For each (log2 triangles, log2 grid edge) bucket of a sweep of displaced spheres and grids, the tuner
 times whole device-buffer bakes (CUDA events on the bake's stream, median of `reps`) under a
-coordinate descent over the three parameters, then fills every bucket of the table from the
-nearest measured one and writes "tri_bucket grid_bucket leaf tile stack" lines (tile 0-based) that
+coordinate descent over the four parameters, then fills every bucket of the table from the
+nearest measured one and writes "tri_bucket grid_bucket leaf tile stack budget" lines (tile
+0-based, budget 0 = never) that
 the library reads at context creation (tuning/gb300.tsv beside lib/, or the file SDFB_TUNING names).
 
     python italy-rs_gb300/sdfb/autotune.py [--out PATH] [--quick]
@@ -30,7 +33,8 @@ DEFAULT_OUT = os.path.join(os.path.dirname(HERE), "tuning", "gb300.tsv")
 TILES = (1, 2, 3, 4, 5, 6)
 LEAVES = (1, 2, 3, 4, 6, 8)
 STACKS = (32, 64)
-START = (4, 3, 64)  # leaf, tile id (1-based), stack: the built-in defaults
+BUDGETS = (-1, 512, 1024, 2048, 4096)
+START = (4, 3, 64, 1024)  # leaf, tile id (1-based), stack, step budget: the built-in defaults
 
 # (icosphere level, grid edge): 1,280 .. 327,680 triangles on 64^3 .. 512^3 grids
 SWEEP = [(3, 64), (3, 128), (3, 256), (4, 64), (4, 128), (4, 256), (5, 128), (5, 256), (5, 512),
@@ -72,15 +76,16 @@ def write_table(path: str, table: dict, measured: dict, times: dict, header: lis
     with open(path, "w") as f:
         for h in header:
             f.write(f"# {h}\n")
-        f.write("# tri_bucket grid_bucket leaf tile(0-based) stack\n")
-        for (tb, nb), (leaf, tile, stack) in sorted(table.items()):
+        f.write("# tri_bucket grid_bucket leaf tile(0-based) stack budget(0 = never)\n")
+        for (tb, nb), (leaf, tile, stack, budget) in sorted(table.items()):
             note = f"  # measured {times[(tb, nb)]:.3f} ms" if (tb, nb) in measured else ""
-            f.write(f"{tb} {nb} {leaf} {tile - 1} {stack}{note}\n")
+            f.write(f"{tb} {nb} {leaf} {tile - 1} {stack} {max(budget, 0)}{note}\n")
 
 
 def _time_bake(ctx, torch, sdfb, dev, grid, params, reps: int) -> float:
-    leaf, tile, stack = params
-    opts = sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY, leaf_size=leaf, tile=tile, stack_depth=stack)
+    leaf, tile, stack, budget = params
+    opts = sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY, leaf_size=leaf, tile=tile, stack_depth=stack,
+                          step_budget=budget)
     stream = torch.cuda.current_stream()
     dv, nv, di, nt, dd, do = dev
     ctx.bake_device(dv, nv, di, nt, grid, opts, dd, do, stream.cuda_stream)  # warm-up
@@ -97,7 +102,7 @@ def _time_bake(ctx, torch, sdfb, dev, grid, params, reps: int) -> float:
 
 
 def tune_case(ctx, torch, sdfb, dev, grid, reps: int, log=print):
-    """Coordinate descent: tile, then leaf, then stack, then tile again. Returns (params, ms)."""
+    """Coordinate descent: tile, leaf, stack, budget, then tile again. Returns (params, ms)."""
     cache = {}
 
     def t(p):
@@ -106,14 +111,15 @@ def tune_case(ctx, torch, sdfb, dev, grid, reps: int, log=print):
         return cache[p]
 
     best = START
-    for axis, values in ((1, TILES), (0, LEAVES), (2, STACKS), (1, TILES)):
+    for axis, values in ((1, TILES), (0, LEAVES), (2, STACKS), (3, BUDGETS), (1, TILES)):
         for v in values:
             p = list(best)
             p[axis] = v
             p = tuple(p)
             if t(p) < t(best):
                 best = p
-    log(f"    {len(cache)} configurations, best leaf {best[0]} tile {best[1]} stack {best[2]}: {t(best):.3f} ms "
+    log(f"    {len(cache)} configurations, best leaf {best[0]} tile {best[1]} stack {best[2]} budget {best[3]}: "
+        f"{t(best):.3f} ms "
         f"(defaults {t(START):.3f} ms)")
     return best, t(best)
 

@@ -280,3 +280,27 @@ def batch_meshes(count: int = 64, seed: int = 2024, tri_lo: float = 1e3, tri_hi:
         v, f = mesh_for_count(target, seed + i + 7919)
         out.append((v, f, n))
     return out
+
+
+def random_materials(ntris: int, seed: int, num_materials: int = 4, tex_sizes=((16, 8), (5, 7)),
+                     short_tri_mat: bool = True) -> dict:
+    """A seeded material set for a soup of `ntris` triangles, in the layout of MeshAsset's
+    materials (src/io/mesh_asset.h:33-54): per material a base colour factor, metallic, roughness
+    and a base colour texture (-1 = none); per triangle a material index (some past the end, which
+    the bake maps to material 0, and the list one short so the last triangle uses the default);
+    one uv pair per soup vertex, spread over [-2, 3) so texture wrapping is exercised; RGBA8
+    textures, the first sRGB-encoded and the second linear."""
+    rng = np.random.default_rng(seed)
+    mat_f = np.empty((num_materials, 5), np.float32)
+    mat_f[:, :3] = rng.uniform(0.0, 1.2, (num_materials, 3))
+    mat_f[:, 3] = rng.uniform(0.0, 1.0, num_materials)
+    mat_f[:, 4] = rng.uniform(0.0, 1.0, num_materials)
+    mat_tex = np.array([(i % (len(tex_sizes) + 1)) - 1 for i in range(num_materials)], np.int32)
+    if num_materials > 1:
+        mat_tex[1] = len(tex_sizes) + 3  # an index past the texture list: no texture
+    tri_mat = rng.integers(0, num_materials + 2, ntris).astype(np.uint32)
+    if short_tri_mat and ntris > 0:
+        tri_mat = tri_mat[:-1]
+    uvs = rng.uniform(-2.0, 3.0, (3 * ntris, 2)).astype(np.float32)
+    textures = [(rng.integers(0, 256, (h, w, 4)).astype(np.uint8), k == 0) for k, (w, h) in enumerate(tex_sizes)]
+    return {"mat_f": mat_f, "mat_tex": mat_tex, "tri_mat": tri_mat, "uvs": uvs, "textures": textures}

@@ -10,6 +10,15 @@
  *                          occupancy = (count > 0) as at :115,121-122
  *   orc_voxelize_sparse    voxelizeMesh, src/convert/voxelize.cpp:52-107 (insertion-ordered cells)
  *   sat_overlap            triBoxOverlap, src/convert/tri_box_overlap.h:12-114 (FP32, same rounding)
+ *   orc_materials_dense    per-cell material averages of bakePerCellMaterial,
+ *                          sdf_baker.cpp:76-128, with triangleMaterial / sampleColorNearest /
+ *                          srgbToLinear of sdf_baker.cpp:42-74
+ *   orc_voxelize_colors    voxelizeMesh's per-cell colours, voxelize.cpp:12-37,52-107
+ *   orc_sample_sdf,        the renderer's consumption of a baked grid: sampleSdf and
+ *   orc_trace_sdf          __intersection__sdf with its slab test, src/render/kernels/
+ *                          pathtracer.cu:587-613,684-702,740-787 (one IEEE operation per
+ *                          operation, no contraction), and orc_ray_mesh, the exact FP64 first
+ *                          ray/triangle hit (Moller & Trumbore, 1997) they are checked against
  *   orc_weld               weldPositions, src/io/mesh_weld.cpp:26-48
  *   orc_watertight         isWatertight, src/io/mesh_validate.cpp:21-59
  * and, because the reference's own distance/sign is an OptiX ray-cast estimate
@@ -296,11 +305,132 @@ int32_t orc_watertight(const uint32_t *welded, int64_t ntris, int64_t *boundary_
   return (boundary == 0 && nonman == 0) ? 1 : 0;
 }
 
+/* ------------------------------------------------------------------------------------------ */
+/* Materials: per-triangle material (sdf_baker.cpp:42-74; the same sampling as voxelize.cpp:12-37) */
+/* and per-cell averages (sdf_baker.cpp:76-128, voxelize.cpp:52-107).                             */
+
+typedef struct {
+  const float *mat_f;     /* 5 per material: base colour r, g, b, metallic, roughness */
+  const int32_t *mat_tex; /* base colour texture per material, -1 = none */
+  int64_t nmat;           /* >= 1 */
+  const uint32_t *tri_mat;
+  int64_t ntri_mat;       /* may be < ntris (missing entries use material 0) */
+  const float *uvs;       /* 2 floats per soup vertex */
+  int64_t nuv;            /* uv pairs */
+  const uint8_t *pixels;  /* every texture's RGBA8 texels, concatenated */
+  const int64_t *tex_off; /* byte offset of each texture in pixels */
+  const int32_t *tex_w, *tex_h, *tex_srgb;
+  int64_t ntex;
+} orc_materials;
+
+/* srgbToLinear (sdf_baker.cpp:42, voxelize.cpp:12). */
+static float srgb_to_linear(float c) { return c <= 0.04045f ? c / 12.92f : powf((c + 0.055f) / 1.055f, 2.4f); }
+
+/* float -> int as static_cast (truncation) for the texel coordinate; NaN -> 0 as f2i_sat. */
+static inline int f2i_trunc(float f) { return f2i_sat(f); }
+
+/* triangleMaterial (sdf_baker.cpp:61-74): out = base colour r, g, b, metallic, roughness. */
+void orc_triangle_material(const orc_materials *m, int64_t t, float *out) {
+  const int64_t mi0 = t < m->ntri_mat ? (int64_t)m->tri_mat[t] : 0;
+  const int64_t mi = mi0 < m->nmat ? mi0 : 0;
+  const float *f = m->mat_f + 5 * mi;
+  float r = f[0], g = f[1], b = f[2];
+  const int32_t tex = m->mat_tex[mi];
+  const int64_t base = t * 3;
+  if (tex >= 0 && tex < m->ntex && base + 2 < m->nuv) {
+    const int32_t w = m->tex_w[tex], h = m->tex_h[tex];
+    if (w > 0 && h > 0) {
+      const float *u = m->uvs + 2 * base;
+      const float uu = ((u[0] + u[2]) + u[4]) / 3.0f, vv = ((u[1] + u[3]) + u[5]) / 3.0f;
+      const float wu = uu - floorf(uu), wv = vv - floorf(vv);
+      const int px = clampi(f2i_trunc(wu * (float)w), 0, w - 1);
+      const int py = clampi(f2i_trunc(wv * (float)h), 0, h - 1);
+      const uint8_t *p = m->pixels + m->tex_off[tex] + ((int64_t)py * w + px) * 4;
+      float cr = (float)p[0] / 255.0f, cg = (float)p[1] / 255.0f, cb = (float)p[2] / 255.0f;
+      if (m->tex_srgb[tex]) {
+        cr = srgb_to_linear(cr);
+        cg = srgb_to_linear(cg);
+        cb = srgb_to_linear(cb);
+      }
+      r = cr * f[0];
+      g = cg * f[1];
+      b = cb * f[2];
+    }
+  }
+  out[0] = r; out[1] = g; out[2] = b; out[3] = f[3]; out[4] = f[4];
+}
+
+/* bakePerCellMaterial (sdf_baker.cpp:76-128) over an explicit grid. Sums start at 0 and add in
+ * triangle order; cells without a hit keep (1, 1, 1), metallic 0, roughness 1. color_out holds 3
+ * floats per cell. Returns 0, -1 on OOM. */
+int32_t orc_materials_dense(const float *soup, int64_t ntris, const float *origin, float voxel, int32_t nx,
+                            int32_t ny, int32_t nz, const orc_materials *m, float *color_out, float *metal_out,
+                            float *rough_out) {
+  const int64_t cells = (int64_t)nx * ny * nz;
+  float *sum = (float *)calloc((size_t)cells * 5, sizeof(float));
+  int32_t *cnt = (int32_t *)calloc((size_t)cells, sizeof(int32_t));
+  if (!sum || !cnt) { free(sum); free(cnt); return -1; }
+  const int nmax[3] = {nx - 1, ny - 1, nz - 1};
+  const float half = voxel * 0.5f;
+  const f3 h = {half, half, half};
+  for (int64_t t = 0; t < ntris; ++t) {
+    const f3 p0 = vtx(soup, NULL, t, 0), p1 = vtx(soup, NULL, t, 1), p2 = vtx(soup, NULL, t, 2);
+    int lo[3], hi[3];
+    tri_cell_range(p0, p1, p2, origin, voxel, nmax, lo, hi);
+    float mat[5];
+    orc_triangle_material(m, t, mat);
+    for (int z = lo[2]; z <= hi[2]; ++z)
+      for (int y = lo[1]; y <= hi[1]; ++y)
+        for (int x = lo[0]; x <= hi[0]; ++x) {
+          const f3 c = {cell_center(origin[0], x, voxel), cell_center(origin[1], y, voxel),
+                        cell_center(origin[2], z, voxel)};
+          if (!sat_overlap(c, h, p0, p1, p2)) continue;
+          const int64_t i = ((int64_t)z * ny + y) * nx + x;
+          for (int k = 0; k < 5; ++k) sum[5 * i + k] += mat[k];
+          cnt[i] += 1;
+        }
+  }
+  for (int64_t i = 0; i < cells; ++i) {
+    if (cnt[i] == 0) {
+      color_out[3 * i] = color_out[3 * i + 1] = color_out[3 * i + 2] = 1.0f;
+      metal_out[i] = 0.0f;
+      rough_out[i] = 1.0f;
+      continue;
+    }
+    const float n = (float)cnt[i];
+    for (int k = 0; k < 3; ++k) color_out[3 * i + k] = sum[5 * i + k] / n;
+    metal_out[i] = sum[5 * i + 3] / n;
+    rough_out[i] = sum[5 * i + 4] / n;
+  }
+  free(sum);
+  free(cnt);
+  return 0;
+}
+
 /* voxelizeMesh (voxelize.cpp:52-107): origin = boundsMin (no pad), voxel = longest / res, every
  * axis clamped to res - 1, cells listed in first-insertion order. Returns the cell count (cells
  * beyond cap are counted, not written), -1 on OOM. */
+static int64_t voxelize_sparse(const float *soup, int64_t ntris, const float *bmin, const float *bmax, int32_t res,
+                               const orc_materials *mats, int32_t *cells_out, float *colors_out, int64_t cap,
+                               float *origin_out, float *voxel_out);
+
 int64_t orc_voxelize_sparse(const float *soup, int64_t ntris, const float *bmin, const float *bmax, int32_t res,
                             int32_t *cells_out, int64_t cap, float *origin_out, float *voxel_out) {
+  return voxelize_sparse(soup, ntris, bmin, bmax, res, NULL, cells_out, NULL, cap, origin_out, voxel_out);
+}
+
+/* voxelizeMesh with its colours (voxelize.cpp:78-104): a cell's sum starts at the colour of the
+ * first triangle that inserts it and adds later ones in triangle order; colour = sum / count.
+ * colors_out holds 3 floats per written cell. */
+int64_t orc_voxelize_colors(const float *soup, int64_t ntris, const float *bmin, const float *bmax, int32_t res,
+                            const orc_materials *mats, int32_t *cells_out, float *colors_out, int64_t cap,
+                            float *origin_out, float *voxel_out) {
+  return voxelize_sparse(soup, ntris, bmin, bmax, res, mats, cells_out, colors_out, cap, origin_out, voxel_out);
+}
+
+static int64_t voxelize_sparse(const float *soup, int64_t ntris, const float *bmin, const float *bmax, int32_t res,
+                               const orc_materials *mats, int32_t *cells_out, float *colors_out, int64_t cap,
+                               float *origin_out, float *voxel_out) {
   const float ex = bmax[0] - bmin[0], ey = bmax[1] - bmin[1], ez = bmax[2] - bmin[2];
   float longest = ex;
   if (longest < ey) longest = ey;
@@ -313,11 +443,21 @@ int64_t orc_voxelize_sparse(const float *soup, int64_t ntris, const float *bmin,
   const f3 h = {half, half, half};
   hmap m;
   if (hmap_init(&m, ntris * 4 + 16, 3)) return -1;
+  const int with_colors = mats && colors_out;
+  float *csum = NULL;
+  int32_t *ccnt = NULL;
+  if (with_colors && cap > 0) {
+    csum = (float *)malloc((size_t)cap * 3 * sizeof(float));
+    ccnt = (int32_t *)malloc((size_t)cap * sizeof(int32_t));
+    if (!csum || !ccnt) { free(csum); free(ccnt); hmap_free(&m); return -1; }
+  }
   int64_t count = 0;
   for (int64_t t = 0; t < ntris; ++t) {
     const f3 p0 = vtx(soup, NULL, t, 0), p1 = vtx(soup, NULL, t, 1), p2 = vtx(soup, NULL, t, 2);
     int lo[3], hi[3];
     tri_cell_range(p0, p1, p2, origin, voxel, nmax, lo, hi);
+    float mat[5] = {0, 0, 0, 0, 0};
+    if (with_colors) orc_triangle_material(mats, t, mat);
     for (int z = lo[2]; z <= hi[2]; ++z)
       for (int y = lo[1]; y <= hi[1]; ++y)
         for (int x = lo[0]; x <= hi[0]; ++x) {
@@ -338,19 +478,165 @@ int64_t orc_voxelize_sparse(const float *soup, int64_t ntris, const float *bmin,
           }
           const int64_t key[3] = {x, y, z};
           int ins;
-          hmap_get_or_insert(&m, key, count, &ins);
+          const int64_t slot = hmap_get_or_insert(&m, key, count, &ins);
+          const int64_t ci = ins ? count : m.vals[slot];
           if (ins) {
             if (count < cap) {
               cells_out[3 * count] = x; cells_out[3 * count + 1] = y; cells_out[3 * count + 2] = z;
+              if (csum) {
+                csum[3 * count] = mat[0]; csum[3 * count + 1] = mat[1]; csum[3 * count + 2] = mat[2];
+                ccnt[count] = 1;
+              }
             }
             count++;
+          } else if (csum && ci < cap) {
+            csum[3 * ci] += mat[0]; csum[3 * ci + 1] += mat[1]; csum[3 * ci + 2] += mat[2];
+            ccnt[ci] += 1;
           }
         }
   }
   hmap_free(&m);
+  if (csum) {
+    const int64_t n = count < cap ? count : cap;
+    for (int64_t i = 0; i < n; ++i)
+      for (int k = 0; k < 3; ++k) colors_out[3 * i + k] = csum[3 * i + k] / (float)ccnt[i];
+    free(csum);
+    free(ccnt);
+  }
   origin_out[0] = origin[0]; origin_out[1] = origin[1]; origin_out[2] = origin[2];
   *voxel_out = voxel;
   return count;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Consumer check: the renderer's trilinear sample and SDF ray march (pathtracer.cu).          */
+
+typedef struct {
+  const float *dist;
+  float o[3], v;
+  int n[3];
+} sdf_view;
+
+static inline float sdf_at(const sdf_view *g, int x, int y, int z) {
+  return g->dist[((int64_t)z * g->n[1] + y) * g->n[0] + x];
+}
+
+static inline float lerp_ref(float a, float b, float f) { return a * (1.0f - f) + b * f; }
+
+static inline int imax(int a, int b) { return a > b ? a : b; }
+static inline int imin(int a, int b) { return a < b ? a : b; }
+
+/* sampleSdf (pathtracer.cu:684-702) */
+static float sample_sdf(const sdf_view *g, const float p[3]) {
+  float l[3], f[3];
+  int c0[3];
+  for (int a = 0; a < 3; ++a) {
+    l[a] = (p[a] - g->o[a]) / g->v - 0.5f;
+    c0[a] = imax(0, imin(g->n[a] - 2, f2i_sat(floorf(l[a]))));
+    f[a] = fminf(fmaxf(l[a] - (float)c0[a], 0.0f), 1.0f);
+  }
+  const int x0 = c0[0], y0 = c0[1], z0 = c0[2];
+  const float c00 = lerp_ref(sdf_at(g, x0, y0, z0), sdf_at(g, x0 + 1, y0, z0), f[0]);
+  const float c10 = lerp_ref(sdf_at(g, x0, y0 + 1, z0), sdf_at(g, x0 + 1, y0 + 1, z0), f[0]);
+  const float c01 = lerp_ref(sdf_at(g, x0, y0, z0 + 1), sdf_at(g, x0 + 1, y0, z0 + 1), f[0]);
+  const float c11 = lerp_ref(sdf_at(g, x0, y0 + 1, z0 + 1), sdf_at(g, x0 + 1, y0 + 1, z0 + 1), f[0]);
+  const float cc0 = lerp_ref(c00, c10, f[1]);
+  const float cc1 = lerp_ref(c01, c11, f[1]);
+  return lerp_ref(cc0, cc1, f[2]);
+}
+
+static float sample_ray(const sdf_view *g, const float *o, const float *d, float t) {
+  const float p[3] = {o[0] + t * d[0], o[1] + t * d[1], o[2] + t * d[2]};
+  return sample_sdf(g, p);
+}
+
+/* slabTest (pathtracer.cu:587-613) */
+static int slab_test(const float *o, const float *d, const float *lo, const float *hi, float *t0, float *t1) {
+  for (int a = 0; a < 3; ++a) {
+    const float inv = 1.0f / d[a];
+    float tn = (lo[a] - o[a]) * inv, tf = (hi[a] - o[a]) * inv;
+    if (tn > tf) { const float x = tn; tn = tf; tf = x; }
+    if (tn > *t0) *t0 = tn;
+    if (tf < *t1) *t1 = tf;
+    if (*t0 > *t1) return 0;
+  }
+  return 1;
+}
+
+/* __intersection__sdf (pathtracer.cu:740-787): reported hit distance, or -1. */
+static float trace_sdf(const sdf_view *g, const float *o, const float *d, float tmin, float tmax) {
+  const float lo[3] = {g->o[0], g->o[1], g->o[2]};
+  const float hi[3] = {g->o[0] + (float)g->n[0] * g->v, g->o[1] + (float)g->n[1] * g->v,
+                       g->o[2] + (float)g->n[2] * g->v};
+  float t0 = tmin, t1 = tmax;
+  if (!slab_test(o, d, lo, hi, &t0, &t1)) return -1.0f;
+  const float eps = g->v * 0.02f, min_step = g->v * 0.05f, min_adv = g->v * 0.3f;
+  float t = t0, prev_t = t0;
+  float prev = sample_ray(g, o, d, t0);
+  t += fmaxf(fabsf(prev), min_step);
+  for (int i = 1; i < 512 && t <= t1; ++i) {
+    const float dist = sample_ray(g, o, d, t);
+    const int crossed = (prev > 0.0f) != (dist > 0.0f);
+    if ((crossed || fabsf(dist) < eps) && (t - t0) > min_adv) {
+      float hit = t;
+      if (crossed) {
+        float a = prev_t, b = t, fa = prev, fb = dist;
+        for (int k = 0; k < 8; ++k) {
+          const float m = 0.5f * (a + b);
+          const float fm = sample_ray(g, o, d, m);
+          if ((fa > 0.0f) != (fm > 0.0f)) { b = m; fb = fm; } else { a = m; fa = fm; }
+        }
+        const float denom = fa - fb;
+        hit = fabsf(denom) > 1e-9f ? a + (b - a) * (fa / denom) : 0.5f * (a + b);
+      }
+      return fmaxf(hit, t0);
+    }
+    prev_t = t;
+    prev = dist;
+    t += fmaxf(fabsf(dist) * 0.85f, min_step);
+  }
+  return -1.0f;
+}
+
+void orc_sample_sdf(const float *dist, const float *origin, float voxel, int32_t nx, int32_t ny, int32_t nz,
+                    const float *pts, int64_t n, float *out) {
+  const sdf_view g = {dist, {origin[0], origin[1], origin[2]}, voxel, {nx, ny, nz}};
+  for (int64_t i = 0; i < n; ++i) out[i] = sample_sdf(&g, pts + 3 * i);
+}
+
+void orc_trace_sdf(const float *dist, const float *origin, float voxel, int32_t nx, int32_t ny, int32_t nz,
+                   const float *rays, int64_t n, float tmin, float tmax, float *t_out) {
+  const sdf_view g = {dist, {origin[0], origin[1], origin[2]}, voxel, {nx, ny, nz}};
+  for (int64_t i = 0; i < n; ++i) t_out[i] = trace_sdf(&g, rays + 6 * i, rays + 6 * i + 3, tmin, tmax);
+}
+
+/* First hit t > 0 of each ray (origin, direction: 6 floats) with the mesh, in FP64 (Moller &
+ * Trumbore, "Fast, minimum storage ray/triangle intersection", 1997), or -1. Brute force. */
+void orc_ray_mesh(const float *verts, const uint32_t *idx, int64_t ntris, const float *rays, int64_t n,
+                  double *t_out) {
+  for (int64_t r = 0; r < n; ++r) {
+    const double o[3] = {rays[6 * r], rays[6 * r + 1], rays[6 * r + 2]};
+    const double d[3] = {rays[6 * r + 3], rays[6 * r + 4], rays[6 * r + 5]};
+    double best = -1.0;
+    for (int64_t t = 0; t < ntris; ++t) {
+      const f3 A = vtx(verts, idx, t, 0), B = vtx(verts, idx, t, 1), Cc = vtx(verts, idx, t, 2);
+      const double e1[3] = {(double)B.x - A.x, (double)B.y - A.y, (double)B.z - A.z};
+      const double e2[3] = {(double)Cc.x - A.x, (double)Cc.y - A.y, (double)Cc.z - A.z};
+      const double p[3] = {d[1] * e2[2] - d[2] * e2[1], d[2] * e2[0] - d[0] * e2[2], d[0] * e2[1] - d[1] * e2[0]};
+      const double det = e1[0] * p[0] + e1[1] * p[1] + e1[2] * p[2];
+      if (fabs(det) < 1e-300) continue;
+      const double inv = 1.0 / det;
+      const double s[3] = {o[0] - A.x, o[1] - A.y, o[2] - A.z};
+      const double u = (s[0] * p[0] + s[1] * p[1] + s[2] * p[2]) * inv;
+      if (u < 0.0 || u > 1.0) continue;
+      const double q[3] = {s[1] * e1[2] - s[2] * e1[1], s[2] * e1[0] - s[0] * e1[2], s[0] * e1[1] - s[1] * e1[0]};
+      const double v = (d[0] * q[0] + d[1] * q[1] + d[2] * q[2]) * inv;
+      if (v < 0.0 || u + v > 1.0) continue;
+      const double tt = (e2[0] * q[0] + e2[1] * q[1] + e2[2] * q[2]) * inv;
+      if (tt > 0.0 && (best < 0.0 || tt < best)) best = tt;
+    }
+    t_out[r] = best;
+  }
 }
 
 /* ------------------------------------------------------------------------------------------ */

@@ -136,6 +136,29 @@ def main():
         gs.append([*lo, *hi, res, *o, v, *n])
     out["grid_sizing_cases"] = np.array(gs, np.float64)
 
+    # 7. Materials: a random soup with a seeded material set (two textures, one sRGB; triangle
+    # material indices past the end; uvs outside [0, 1)). Sparse colours come from the
+    # reference's own voxelizeMesh; the dense per-cell averages of bakePerCellMaterial from its
+    # restatement in the reference driver (that function sits in the OptiX translation unit).
+    ms = random_soup(400, 21)
+    mm = mg.random_materials(len(ms) // 3, 21)
+    out["mat_soup"] = ms
+    out["mat_f"] = mm["mat_f"]
+    out["mat_tex"] = mm["mat_tex"]
+    out["mat_tri"] = mm["tri_mat"]
+    out["mat_uvs"] = mm["uvs"]
+    out["mat_tex0"], out["mat_tex1"] = mm["textures"][0][0], mm["textures"][1][0]
+    out["mat_tex_srgb"] = np.array([1 if t[1] else 0 for t in mm["textures"]], np.int32)
+    mc, mcol = R.voxelize_colors(ms, ms.min(0), ms.max(0), 40, mm)
+    out["mat_sparse_cells"] = mc
+    out["mat_sparse_colors"] = mcol
+    mo, mv, mn = R.grid_from_bounds(ms.min(0), ms.max(0), 24)
+    col, met, rou = R.materials_dense(ms, mo, mv, mn, mm)
+    hit = np.flatnonzero(np.any(col != 1.0, axis=1) | (met != 0.0) | (rou != 1.0)).astype(np.int64)
+    out["mat_dense_grid"] = np.array([*mo, mv, *mn], np.float64)
+    out["mat_dense_cells"] = hit
+    out["mat_dense_values"] = np.concatenate([col[hit], met[hit, None], rou[hit, None]], axis=1)
+
     path = os.path.join(HERE, "golden.npz")
     np.savez_compressed(path, **out)
     print(path, os.path.getsize(path), "bytes;", msg2)

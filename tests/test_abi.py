@@ -49,6 +49,21 @@ def test_struct_layout_matches_header(tmp_path):
     assert int(out[4]) == sdfb.Opts.count_work.offset
 
 
+def test_material_struct_layout_matches_header(tmp_path):
+    import sdfb
+    src = tmp_path / "msizes.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "sdfb.h"\n'
+                   'int main(void){printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(sdfb_texture), sizeof(sdfb_material),'
+                   ' sizeof(sdfb_materials), offsetof(sdfb_materials, uvs), offsetof(sdfb_materials, num_textures),'
+                   ' offsetof(sdfb_material, base_color_texture));return 0;}\n')
+    exe = tmp_path / "msizes"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert out == [C.sizeof(sdfb.Texture), C.sizeof(sdfb.Material), C.sizeof(sdfb.Materials),
+                   sdfb.Materials.uvs.offset, sdfb.Materials.num_textures.offset,
+                   sdfb.Material.base_color_texture.offset]
+
+
 def test_abi_version(lib):
     assert lib.sdfb_abi_version() == 1
 

@@ -10,14 +10,15 @@ def test_buckets_match_library_rule():
 
 
 def test_fill_table_nearest(tmp_path):
-    measured = {(10, 2): (2, 1, 32), (16, 4): (4, 3, 64)}
+    measured = {(10, 2): (2, 1, 32, -1), (16, 4): (4, 3, 64, 1024)}
     table = autotune.fill_table(measured)
     assert len(table) == 32 * 8
-    assert table[(10, 2)] == (2, 1, 32) and table[(16, 4)] == (4, 3, 64)
-    assert table[(0, 0)] == (2, 1, 32) and table[(31, 7)] == (4, 3, 64)
+    assert table[(10, 2)] == (2, 1, 32, -1) and table[(16, 4)] == (4, 3, 64, 1024)
+    assert table[(0, 0)] == (2, 1, 32, -1) and table[(31, 7)] == (4, 3, 64, 1024)
     path = tmp_path / "t.tsv"
     autotune.write_table(str(path), table, measured, {(10, 2): 1.0, (16, 4): 2.0}, ["test"])
     rows = [l.split("#")[0].split() for l in path.read_text().splitlines() if not l.startswith("#")]
     assert len(rows) == 256
     row = [r for r in rows if r[:2] == ["16", "4"]][0]
-    assert row == ["16", "4", "4", "2", "64"]  # tile written 0-based
+    assert row == ["16", "4", "4", "2", "64", "1024"]  # tile written 0-based
+    assert [r for r in rows if r[:2] == ["10", "2"]][0][5] == "0"  # never defer

@@ -244,3 +244,24 @@ def test_device_entry_point_matches_host(ctx):
     ctx.bake_device(dv.data_ptr(), len(v), di.data_ptr(), len(i), g, sdfb.make_opts(), dd.data_ptr(), do.data_ptr())
     assert np.array_equal(dd.cpu().numpy().reshape(hd.shape), hd)
     assert np.array_equal(do.cpu().numpy().reshape(ho.shape), ho)
+
+
+@pytest.mark.parametrize("tile", [1, 3, 6])
+def test_deferred_tiles_agree(ctx, tile):
+    """Tiles still walking when every tile has been handed out are finished by a block-per-tile
+    pass that splits the tree into subtrees; the result must not depend on it. With a budget of 8
+    steps nearly every tile in flight at the end is deferred; budget -1 defers none."""
+    import sdfb
+    from sdfb import meshgen as mg
+    v, i = mg.displaced_icosphere(5, 0.4, 7)
+    g = sdfb.make_grid((-0.5,) * 3, 1.0 / 128, (128, 128, 128))
+    out = {}
+    for budget in (-1, 8):
+        st = sdfb.Stats()
+        st.struct_size = sdfb.C.sizeof(sdfb.Stats)
+        d, o = ctx.bake(v, i, g, sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY, tile=tile, step_budget=budget), stats=st)
+        out[budget] = (d, o, st.tiles_deferred)
+    assert out[-1][2] == 0 and out[8][2] > 100
+    assert np.array_equal(out[-1][1], out[8][1])
+    # the same nearest triangle; a culling decision on an FP32 box bound may only differ by rounding
+    assert np.abs(out[-1][0] - out[8][0]).max() <= 4e-7 and np.array_equal(out[-1][0] < 0, out[8][0] < 0)

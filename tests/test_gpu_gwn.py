@@ -71,3 +71,34 @@ def test_gwn_band_width_option(ctx):
     d3, _ = ctx.bake(v, f, grid, sdfb.make_opts(sign_mode=sdfb.SIGN_GWN, band_voxels=3.0), stats=s3)
     assert s3.gwn_fp64_cells > s1.gwn_fp64_cells
     assert np.array_equal(np.abs(d1), np.abs(d3))
+
+
+def test_c3_soup_full_size(ctx, oracle):
+    """The 500k-triangle soup with 2% of its faces deleted, on the 512^3 grid: occupancy on every
+    cell, distance on a seeded 20,000-cell sample against FP64, winding-number sign on a seeded
+    sample of 3,000 cells outside the band and 1,000 band cells against the FP64 direct sum."""
+    import sdfb
+    from sdfb import meshgen as mg
+    v, f = mg.soup_with_holes()
+    n = (512, 512, 512)
+    origin, voxel = (-0.5,) * 3, 1.0 / 512
+    g = sdfb.make_grid(origin, voxel, n)
+    st = sdfb.Stats()
+    st.struct_size = sdfb.C.sizeof(sdfb.Stats)
+    dist, occ = ctx.bake(v, f, g, sdfb.make_opts(sign_mode=sdfb.SIGN_AUTO), stats=st)
+    assert st.sign_mode_used == sdfb.SIGN_GWN and st.watertight == 0
+    assert np.array_equal(occ.reshape(-1), oracle.occupancy(v, f, origin, voxel, n))
+    flat = dist.reshape(-1)
+    rng = np.random.default_rng(33)
+    samp = np.sort(rng.choice(flat.size, 20000, replace=False)).astype(np.int64)
+    d64 = oracle.distance(v, f, origin, voxel, n, samples=samp)
+    assert np.abs(np.abs(flat[samp].astype(np.float64)) - d64).max() <= DIST_TOL * np.sqrt(3)
+    far = samp[d64 > voxel][:3000]
+    w = oracle.gwn(v, f, origin, voxel, n, samples=far)
+    ok = np.abs(np.abs(w) - 0.5) > 1e-6
+    assert np.count_nonzero((flat[far][ok] < 0) != (np.abs(w[ok]) > 0.5)) == 0
+    band = np.flatnonzero(np.abs(flat) <= voxel)
+    band = np.sort(rng.choice(band, min(1000, band.size), replace=False)).astype(np.int64)
+    wb = oracle.gwn(v, f, origin, voxel, n, samples=band)
+    okb = np.abs(np.abs(wb) - 0.5) > 1e-6
+    assert np.count_nonzero((flat[band][okb] < 0) != (np.abs(wb[okb]) > 0.5)) <= 2

@@ -87,3 +87,42 @@ def test_pinned_outputs(ctx):
         assert srv.poll(rid, 60000)[0]
     d1, o1 = ctx.bake(v, f, g, sdfb.make_opts())
     assert np.array_equal(d, d1) and np.array_equal(o, o1)
+
+
+def test_concurrent_registration_of_the_same_mesh(ctx):
+    """Many threads register the same few meshes at once and submit right away (the serving
+    stream's repeats): each mesh is built once, and every result equals the plain bake."""
+    import threading
+
+    import sdfb
+    from sdfb import meshgen as mg
+    meshes = [mg.displaced_icosphere(4, 0.3, 21), mg.displaced_torus(60, 20, 0.27, 0.1, 22)]
+    n = 40
+    g = sdfb.make_grid((-0.5,) * 3, 1.0 / n, (n, n, n))
+    ref = [ctx.bake(v, f, g, sdfb.make_opts()) for v, f in meshes]
+    errors, results = [], []
+    with sdfb.Server(ctx, max_inflight=8, wave_voxels_log2=18) as srv:
+        start = threading.Barrier(16)
+
+        def worker(k):
+            try:
+                v, f = meshes[k % 2]
+                start.wait()
+                mid = srv.register(v, f)
+                d = np.empty(g.shape, np.float32)
+                o = np.empty(g.shape, np.uint8)
+                done, info = srv.poll(srv.submit(mid, g, d, o), 60000)
+                results.append((k % 2, done, info["status"], d, o))
+            except Exception as e:  # reported below
+                errors.append(repr(e))
+
+        threads = [threading.Thread(target=worker, args=(k,)) for k in range(16)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+    assert not errors, errors[0]
+    assert len(results) == 16
+    for m, done, status, d, o in results:
+        assert done and status == 0
+        assert np.array_equal(d, ref[m][0]) and np.array_equal(o, ref[m][1])

@@ -208,3 +208,52 @@ def test_degenerate_triangles_are_their_edges(oracle):
     V = v.astype(np.float64)
     bf = np.minimum.reduce([seg(V[0], V[2]), seg(V[3], V[0]), seg(V[2], V[2])])
     assert np.abs(bf - d).max() < 1e-12
+
+
+def golden_materials(golden):
+    return {"mat_f": golden["mat_f"], "mat_tex": golden["mat_tex"], "tri_mat": golden["mat_tri"],
+            "uvs": golden["mat_uvs"],
+            "textures": [(golden["mat_tex0"], bool(golden["mat_tex_srgb"][0])),
+                         (golden["mat_tex1"], bool(golden["mat_tex_srgb"][1]))]}
+
+
+def test_material_colors_match_reference(golden, oracle):
+    """voxelizeMesh's per-cell colours (voxelize.cpp:78-104, textures sampled nearest with wrap,
+    sRGB decoded) and bakePerCellMaterial's dense averages (sdf_baker.cpp:76-128), bit for bit."""
+    soup, m = golden["mat_soup"], golden_materials(golden)
+    cells, cols = oracle.voxelize_colors(soup, soup.min(0), soup.max(0), 40, m)
+    assert np.array_equal(cells, golden["mat_sparse_cells"])
+    assert np.array_equal(cols.view(np.uint32), golden["mat_sparse_colors"].view(np.uint32))
+    # the same cell list as the plain voxelizer
+    plain, _, _ = oracle.voxelize_sparse(soup, soup.min(0), soup.max(0), 40)
+    assert np.array_equal(plain, cells)
+    g = golden["mat_dense_grid"]
+    col, met, rou = oracle.materials_dense(soup, g[0:3].astype(np.float32), np.float32(g[3]),
+                                           tuple(int(x) for x in g[4:7]), m)
+    hit = golden["mat_dense_cells"]
+    got = np.concatenate([col[hit], met[hit, None], rou[hit, None]], axis=1)
+    assert np.array_equal(got.view(np.uint32), golden["mat_dense_values"].view(np.uint32))
+    rest = np.ones(len(met), bool)
+    rest[hit] = False
+    assert (col[rest] == 1.0).all() and (met[rest] == 0.0).all() and (rou[rest] == 1.0).all()
+    # textures matter: some cells average textured colours, which differ from every factor
+    assert len(np.unique(cols[:, 0])) > len(golden["mat_f"])
+
+
+def test_oracle_matches_live_reference_materials(reference, oracle):
+    from sdfb import meshgen as mg
+    rng = np.random.default_rng(17)
+    for seed in range(3):
+        n = int(rng.integers(40, 300))
+        c = rng.uniform(-0.45, 0.45, size=(n, 1, 3))
+        s = rng.lognormal(mean=-2.5, sigma=0.8, size=(n, 1, 1))
+        tri = (c + s * rng.normal(size=(n, 3, 3))).reshape(-1, 3).astype(np.float32)
+        m = mg.random_materials(n, 100 + seed, num_materials=int(rng.integers(1, 6)))
+        lo, hi = tri.min(0), tri.max(0)
+        res = int(rng.integers(6, 40))
+        cr, kr = reference.voxelize_colors(tri, lo, hi, res, m)
+        co, ko = oracle.voxelize_colors(tri, lo, hi, res, m)
+        assert np.array_equal(cr, co) and np.array_equal(kr.view(np.uint32), ko.view(np.uint32))
+        o, v, nn = reference.grid_from_bounds(lo, hi, res)
+        for a, b in zip(reference.materials_dense(tri, o, v, nn, m), oracle.materials_dense(tri, o, v, nn, m)):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
