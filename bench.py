@@ -345,6 +345,8 @@ def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, re
         return (v + np.asarray(off, np.float32)).astype(np.float32), f
 
     failures = []
+    dropped = []
+    deadline = [float("inf")]  # requests not started by then are dropped (reported, never timed)
 
     def worker():
         while True:
@@ -352,6 +354,10 @@ def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, re
             if item is None:
                 return
             k, arrival = item
+            if time.monotonic() > deadline[0]:
+                with lock:
+                    dropped.append(k)
+                continue
             _, key, n = reqs[k]
             v, f = mesh_of(key)
             slot = slots.get()
@@ -386,6 +392,7 @@ def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, re
     d0, o0 = slot_bufs[0]
     srv.poll(srv.submit(srv.register(v0, f0), g0, d0[:g0.cells], o0[:g0.cells]), 120000)
     t0 = time.monotonic()
+    deadline[0] = t0 + seconds + max(60.0, seconds)
     for k, (arr, key, n) in enumerate(reqs):
         now = time.monotonic() - t0
         if arr > now:
@@ -398,13 +405,16 @@ def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, re
     srv.close()
     if failures:
         print(f"serve_stream: {len(failures)} requests failed, first: {failures[0]}", file=sys.stderr)
+    if dropped:
+        print(f"serve_stream: {len(dropped)} requests dropped at the drain deadline", file=sys.stderr)
     lat = [r[2] - r[0] for r in results if r]
     done = [r for r in results if r and r[4] == 0]
     if not done:
         raise RuntimeError(f"serve_stream: no request completed ({len(failures)} failed)")
     span = max(r[2] for r in done) - t0
     vox = sum(r[3] for r in done)
-    return {"requests": len(reqs), "completed": len(done), "failed": len(reqs) - len(done), "new_meshes": len(news),
+    return {"requests": len(reqs), "completed": len(done), "failed": len(failures), "dropped": len(dropped),
+            "new_meshes": len(news),
             "voxels_per_s": vox / span, "p50_ms": 1e3 * percentile(lat, 50), "p99_ms": 1e3 * percentile(lat, 99),
             "mean_ms": 1e3 * statistics.mean(lat), "seconds": span, "rate_per_s": rate, "repeat_fraction": repeat,
             "hbm_budget_gb": 150}, reqs
@@ -418,8 +428,12 @@ def plain_stream(sdfb, ctx, base_meshes, reqs, seconds):
     lat, vox = [], 0
     t0 = time.monotonic()
     opts = sdfb.make_opts(sign_mode=sdfb.SIGN_AUTO)
+    limit = max(60.0, 6 * seconds)  # wall-clock cap; requests not reached by then are not counted
+    done = 0
     for arr, (b, off), n in sub:
         now = time.monotonic() - t0
+        if now > limit:
+            break
         if arr > now:
             time.sleep(arr - now)
         v, f, _ = base_meshes[b]
@@ -428,8 +442,9 @@ def plain_stream(sdfb, ctx, base_meshes, reqs, seconds):
         ctx.bake(v, f, g, opts)
         lat.append(time.monotonic() - t0 - arr)
         vox += g.cells
+        done += 1
     span = time.monotonic() - t0
-    return {"requests": len(sub), "voxels_per_s": vox / span, "p50_ms": 1e3 * percentile(lat, 50),
+    return {"requests": len(sub), "completed": done, "voxels_per_s": vox / span, "p50_ms": 1e3 * percentile(lat, 50),
             "p99_ms": 1e3 * percentile(lat, 99), "seconds": span,
             "note": f"arrivals of the first {seconds:.0f} s of the same stream, one sdfb_bake per request"}
 

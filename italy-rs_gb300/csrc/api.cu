@@ -205,6 +205,22 @@ sdfb_status upload_caps(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &m
 
 }  // namespace
 
+sdfb_status device_sign(sdfb_ctx *ctx, const sdfb_opts &o, const float *d_verts, uint32_t V, const uint32_t *d_idx,
+                        uint32_t T, cudaStream_t st, int *sign, int *watertight) {
+  *watertight = -1;
+  if (o.sign_mode != SDFB_SIGN_AUTO) {
+    *sign = resolve_sign(o, nullptr, 0, nullptr, 0, watertight);
+    return SDFB_OK;
+  }
+  ENSURE(ctx->weld_tmp, indexed_gate_temp_bytes(V, T));
+  int w = 0;
+  CK(indexed_watertight_device(d_verts, V, d_idx, T, ctx->weld_tmp.p, ctx->weld_tmp.cap, &w, ctx->num_sms, st));
+  if (w == -2) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "triangle index out of range");
+  *watertight = w == 1 ? 1 : 0;
+  *sign = w == 1 ? kSignParity : kSignGwn;
+  return SDFB_OK;
+}
+
 // ---------------------------------------------------------------------------------------------
 // C ABI.
 
@@ -309,26 +325,19 @@ sdfb_status sdfb_bake_device(sdfb_ctx *ctx, const float *d_verts, uint32_t num_v
   p.dist = o.no_distance ? nullptr : d_dist_out;
   p.occ = o.no_occupancy ? nullptr : d_occ_out;
   std::vector<CapBuild> caps(1);
-  if (o.sign_mode == SDFB_SIGN_AUTO || o.sign_mode == SDFB_SIGN_GWN) {
-    // the watertight gate and the caps need the mesh on the host
+  sdfb_status s = device_sign(ctx, o, d_verts, num_verts, d_idx, num_tris, st, &p.sign, &p.watertight);
+  if (s != SDFB_OK) return s;
+  if (p.sign == kSignGwn && p.dist) {
+    // the caps are built on the host
     std::vector<float> hv(size_t(num_verts) * 3);
     std::vector<uint32_t> hi(size_t(num_tris) * 3);
     CK(cudaMemcpyAsync(hv.data(), d_verts, hv.size() * 4, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(hi.data(), d_idx, hi.size() * 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    p.sign = resolve_sign(o, hv.data(), num_verts, hi.data(), num_tris, &p.watertight);
-    if (p.sign < 0) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "triangle index out of range");
-    if (p.sign == kSignGwn && p.dist) {
-      for (size_t k = 0; k < hi.size(); ++k)
-        if (hi[k] >= num_verts) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "triangle index out of range");
-      build_caps(hv.data(), num_verts, hi.data(), num_tris, caps[0]);
-    }
-  } else {
-    p.sign = resolve_sign(o, nullptr, 0, nullptr, 0, &p.watertight);
-  }
-  if (p.sign == kSignGwn && p.dist) {
-    const sdfb_status s = upload_caps(ctx, st, ms, caps);
-    if (s != SDFB_OK) return s;
+    for (size_t k = 0; k < hi.size(); ++k)
+      if (hi[k] >= num_verts) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "triangle index out of range");
+    build_caps(hv.data(), num_verts, hi.data(), num_tris, caps[0]);
+    if ((s = upload_caps(ctx, st, ms, caps)) != SDFB_OK) return s;
   }
   return run_batch(ctx, st, ms, o, false, stats);
 }
@@ -346,22 +355,23 @@ sdfb_status sdfb_bake(sdfb_ctx *ctx, const float *verts, uint32_t num_verts, con
   const cudaStream_t st = ctx->stream;
   std::vector<PlanMesh> ms(1);
   PlanMesh &p = ms[0];
-  p.sign = resolve_sign(o, verts, num_verts, idx, num_tris, &p.watertight);
-  if (p.sign < 0) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "triangle index out of range");
   const uint64_t cells = uint64_t(grid->nx) * grid->ny * grid->nz;
   const bool want_dist = dist_out && !o.no_distance, want_occ = occ_out && !o.no_occupancy;
-  std::vector<CapBuild> caps(1);
-  if (p.sign == kSignGwn && want_dist) {
-    for (size_t k = 0; k < size_t(num_tris) * 3; ++k)
-      if (idx[k] >= num_verts) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "triangle index out of range");
-    build_caps(verts, num_verts, idx, num_tris, caps[0]);
-  }
   ENSURE(ctx->in_verts, size_t(num_verts) * 12);
   ENSURE(ctx->in_idx, size_t(num_tris) * 12);
   if (want_dist) ENSURE(ctx->out_dist, cells * 4);
   if (want_occ) ENSURE(ctx->out_occ, cells);
   CK(cudaMemcpyAsync(ctx->in_verts.p, verts, size_t(num_verts) * 12, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(ctx->in_idx.p, idx, size_t(num_tris) * 12, cudaMemcpyHostToDevice, st));
+  sdfb_status sg = device_sign(ctx, o, static_cast<const float *>(ctx->in_verts.p), num_verts,
+                               static_cast<const uint32_t *>(ctx->in_idx.p), num_tris, st, &p.sign, &p.watertight);
+  if (sg != SDFB_OK) return sg;
+  std::vector<CapBuild> caps(1);
+  if (p.sign == kSignGwn && want_dist) {
+    for (size_t k = 0; k < size_t(num_tris) * 3; ++k)
+      if (idx[k] >= num_verts) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "triangle index out of range");
+    build_caps(verts, num_verts, idx, num_tris, caps[0]);
+  }
   p.verts = static_cast<const float *>(ctx->in_verts.p);
   p.idx = static_cast<const uint32_t *>(ctx->in_idx.p);
   p.V = num_verts;
@@ -652,22 +662,21 @@ sdfb_status sdfb_bake_batch_device(sdfb_ctx *ctx, uint32_t count, const sdfb_mes
     p.grid = grids[m];
     p.dist = (o.no_distance || !dist_outs) ? nullptr : dist_outs[m];
     p.occ = (o.no_occupancy || !occ_outs) ? nullptr : occ_outs[m];
-    if (o.sign_mode == SDFB_SIGN_AUTO || o.sign_mode == SDFB_SIGN_GWN) {
+    const sdfb_status sg = device_sign(ctx, o, d.verts, d.num_verts, d.idx, d.num_tris, st, &p.sign, &p.watertight);
+    if (sg != SDFB_OK) {
+      const std::string e = ctx->err;
+      return ctx_fail(ctx, sg, "mesh %u: %s", m, e.c_str());
+    }
+    if (p.sign == kSignGwn && p.dist) {
       std::vector<float> hv(size_t(d.num_verts) * 3);
       std::vector<uint32_t> hi(size_t(d.num_tris) * 3);
       CK(cudaMemcpyAsync(hv.data(), d.verts, hv.size() * 4, cudaMemcpyDeviceToHost, st));
       CK(cudaMemcpyAsync(hi.data(), d.idx, hi.size() * 4, cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
-      p.sign = resolve_sign(o, hv.data(), d.num_verts, hi.data(), d.num_tris, &p.watertight);
-      if (p.sign < 0) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh %u: triangle index out of range", m);
-      if (p.sign == kSignGwn && p.dist) {
-        for (size_t k = 0; k < hi.size(); ++k)
-          if (hi[k] >= d.num_verts) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh %u: triangle index out of range", m);
-        build_caps(hv.data(), d.num_verts, hi.data(), d.num_tris, caps[m]);
-        any_gwn = true;
-      }
-    } else {
-      p.sign = resolve_sign(o, nullptr, 0, nullptr, 0, &p.watertight);
+      for (size_t k = 0; k < hi.size(); ++k)
+        if (hi[k] >= d.num_verts) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh %u: triangle index out of range", m);
+      build_caps(hv.data(), d.num_verts, hi.data(), d.num_tris, caps[m]);
+      any_gwn = true;
     }
   }
   if (any_gwn) {
@@ -710,12 +719,15 @@ sdfb_status sdfb_bake_batch(sdfb_ctx *ctx, uint32_t count, const sdfb_mesh_desc 
   for (uint32_t m = 0; m < count; ++m) {
     const sdfb_mesh_desc &d = meshes[m];
     PlanMesh &p = ms[m];
-    p.sign = resolve_sign(o, d.verts, d.num_verts, d.idx, d.num_tris, &p.watertight);
-    if (p.sign < 0) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh %u: triangle index out of range", m);
     float *dv = static_cast<float *>(ctx->in_verts.p) + ov;
     uint32_t *di = static_cast<uint32_t *>(ctx->in_idx.p) + oi;
     CK(cudaMemcpyAsync(dv, d.verts, size_t(d.num_verts) * 12, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(di, d.idx, size_t(d.num_tris) * 12, cudaMemcpyHostToDevice, st));
+    const sdfb_status sg = device_sign(ctx, o, dv, d.num_verts, di, d.num_tris, st, &p.sign, &p.watertight);
+    if (sg != SDFB_OK) {
+      const std::string e = ctx->err;
+      return ctx_fail(ctx, sg, "mesh %u: %s", m, e.c_str());
+    }
     p.verts = dv;
     p.idx = di;
     p.V = d.num_verts;

@@ -148,6 +148,11 @@ void load_tuning(sdfb_ctx *ctx);
 
 sdfb_status ctx_fail(sdfb_ctx *ctx, sdfb_status st, const char *fmt, ...);
 sdfb_status ctx_cuda(sdfb_ctx *ctx, cudaError_t e, const char *what);
+// Sign mode of a mesh in device memory: forced modes pass through; AUTO runs the weld + watertight
+// gate on the device (parity when watertight, else the winding number). Fails with BAD_MESH on an
+// index out of range.
+sdfb_status device_sign(sdfb_ctx *ctx, const sdfb_opts &o, const float *d_verts, uint32_t V, const uint32_t *d_idx,
+                        uint32_t T, cudaStream_t st, int *sign, int *watertight);
 // sdfb_voxelize_sparse; also returns the device list of the count occupied cells' linear indices
 // (valid until the context's next call) and the grid it used.
 sdfb_status voxelize_sparse_run(sdfb_ctx *ctx, const float *positions, uint32_t num_tris, const float bounds_min[3],

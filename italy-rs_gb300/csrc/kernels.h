@@ -188,6 +188,13 @@ size_t watertight_temp_bytes(uint64_t T);
 cudaError_t watertight_device(const uint32_t *welded, uint64_t T, uint32_t num_unique, void *temp, size_t temp_bytes,
                               uint64_t *boundary, uint64_t *nonmanifold, int num_sms, cudaStream_t st);
 
+// The watertight gate of an indexed mesh on the device (the weld of its vertices over their
+// bounds, then the edge census of the welded triangles; equivalent to the reference's test on the
+// de-indexed soup). *result: 1 watertight, 0 not, -2 an index >= V. Synchronises the stream.
+size_t indexed_gate_temp_bytes(uint64_t V, uint64_t T);
+cudaError_t indexed_watertight_device(const float *verts, uint32_t V, const uint32_t *idx, uint32_t T, void *temp,
+                                      size_t temp_bytes, int *result, int num_sms, cudaStream_t st);
+
 // ---- sparse.cu --------------------------------------------------------------------------------
 size_t sparse_temp_bytes(size_t cells, size_t max_out);
 // Counts occupied cells (synchronises the stream; *h_total is host memory).

@@ -485,20 +485,8 @@ sdfb_status sdfb_mesh_register(sdfb_server *srv, const float *verts, uint32_t nu
   r->id = h;
   r->V = num_verts;
   r->T = num_tris;
-  const int w = indexed_mesh_watertight(verts, num_verts, idx, num_tris);
-  r->watertight = w == 1 ? 1 : 0;
-  r->sign = w == 1 ? kSignParity : kSignGwn;
-  CapBuild caps;
-  if (r->sign == kSignGwn) {
-    build_caps(verts, num_verts, idx, num_tris, caps);
-    r->pV = static_cast<uint32_t>(caps.verts.size() / 3);
-    r->pT = static_cast<uint32_t>(caps.pidx.size() / 3);
-    r->cT = static_cast<uint32_t>(caps.cidx.size() / 3);
-  }
   const size_t bvh_bytes = resident_bytes(num_tris, false);
-  const size_t cap_bytes = r->cT ? resident_bytes(r->cT, true) : 0;
-  r->bytes = size_t(num_verts) * 12 + size_t(num_tris) * 12 + bvh_bytes + cap_bytes +
-             (r->sign == kSignGwn ? caps.verts.size() * 4 + caps.pidx.size() * 4 + caps.cidx.size() * 4 : 0);
+  r->bytes = size_t(num_verts) * 12 + size_t(num_tris) * 12 + bvh_bytes;
   {
     std::lock_guard<std::mutex> g(srv->mu);
     if (!srv->make_room(r->bytes))
@@ -518,7 +506,36 @@ sdfb_status sdfb_mesh_register(sdfb_server *srv, const float *verts, uint32_t nu
     return undo(SDFB_ERR_OUT_OF_MEMORY, "device allocation failed");
   cudaMemcpyAsync(r->verts.p, verts, size_t(num_verts) * 12, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(r->idx.p, idx, size_t(num_tris) * 12, cudaMemcpyHostToDevice, st);
+  // the weld + watertight gate on the device decides the sign mode
+  sdfb_opts auto_opts;
+  std::memset(&auto_opts, 0, sizeof auto_opts);
+  auto_opts.sign_mode = SDFB_SIGN_AUTO;
+  int sign = kSignParity, watertight = -1;
+  const sdfb_status gs = device_sign(srv->reg.get(), auto_opts, static_cast<const float *>(r->verts.p), num_verts,
+                                     static_cast<const uint32_t *>(r->idx.p), num_tris, st, &sign, &watertight);
+  if (gs != SDFB_OK) return undo(gs, srv->reg->err);
+  r->sign = sign;
+  r->watertight = watertight;
+  CapBuild caps;
+  size_t cap_bytes = 0;
   if (r->sign == kSignGwn) {
+    build_caps(verts, num_verts, idx, num_tris, caps);
+    r->pV = static_cast<uint32_t>(caps.verts.size() / 3);
+    r->pT = static_cast<uint32_t>(caps.pidx.size() / 3);
+    r->cT = static_cast<uint32_t>(caps.cidx.size() / 3);
+    cap_bytes = r->cT ? resident_bytes(r->cT, true) : 0;
+    const uint64_t extra = cap_bytes + caps.verts.size() * 4 + caps.pidx.size() * 4 + caps.cidx.size() * 4;
+    {
+      std::lock_guard<std::mutex> g(srv->mu);
+      if (!srv->make_room(extra)) {
+        srv->free_resident(*r, st);
+        cudaStreamSynchronize(st);
+        srv->resident_bytes_used -= r->bytes;
+        return srv->fail(SDFB_ERR_OUT_OF_MEMORY, "mesh does not fit the HBM budget next to in-flight work");
+      }
+      srv->resident_bytes_used += extra;
+      r->bytes += extra;
+    }
     if (!async_alloc(r->pverts, caps.verts.size() * 4, st) || !async_alloc(r->pidx, caps.pidx.size() * 4, st) ||
         !async_alloc(r->cidx, std::max<size_t>(caps.cidx.size(), 1) * 4, st) ||
         (cap_bytes && !async_alloc(r->caps, cap_bytes, st)))

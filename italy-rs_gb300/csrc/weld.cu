@@ -21,6 +21,7 @@
 
 #include "api_internal.h"
 #include "common.cuh"
+#include "host_mesh.h"
 #include "kernels.h"
 
 using namespace sdfb;
@@ -156,6 +157,46 @@ int bits_of(unsigned long long range) {
   return b;
 }
 
+// Vertex bounds as order-preserving unsigned values: out[0..2] minima, out[3..5] maxima.
+__global__ __launch_bounds__(kThreads) void k_bounds(const float *__restrict__ v, uint64_t n,
+                                                     unsigned int *__restrict__ out) {
+  unsigned int lo[3] = {~0u, ~0u, ~0u}, hi[3] = {0, 0, 0};
+  for (uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x; i < n; i += uint64_t(gridDim.x) * kThreads)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const unsigned int u = float_to_ordered(v[3 * i + a]);
+      lo[a] = min(lo[a], u);
+      hi[a] = max(hi[a], u);
+    }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[a] = min(lo[a], __shfl_xor_sync(kFull, lo[a], o));
+      hi[a] = max(hi[a], __shfl_xor_sync(kFull, hi[a], o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(out + a, lo[a]);
+      atomicMax(out + 3 + a, hi[a]);
+    }
+  }
+}
+
+// Triangle corners through the vertex weld; err = 1 when an index is out of range.
+__global__ __launch_bounds__(kThreads) void k_map_tris(const uint32_t *__restrict__ idx, uint64_t n, uint32_t V,
+                                                       const uint32_t *__restrict__ wv, uint32_t *__restrict__ tri,
+                                                       unsigned int *__restrict__ err) {
+  for (uint64_t k = uint64_t(blockIdx.x) * kThreads + threadIdx.x; k < n; k += uint64_t(gridDim.x) * kThreads) {
+    const uint32_t i = idx[k];
+    if (i >= V) {
+      *err = 1;
+      tri[k] = 0;
+    } else {
+      tri[k] = wv[i];
+    }
+  }
+}
+
 __global__ __launch_bounds__(kThreads) void k_gather_unique(const float *__restrict__ pos,
                                                             const uint32_t *__restrict__ first_of, uint64_t U,
                                                             float *__restrict__ out) {
@@ -232,6 +273,52 @@ cudaError_t weld_device(const float *pos, uint64_t n, float cell, uint32_t *weld
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
   *num_unique = static_cast<uint32_t>(total);
   return cudaGetLastError();
+}
+
+size_t indexed_gate_temp_bytes(uint64_t V, uint64_t T) {
+  return align256(64) + align256(V * 4) + align256(T * 12) + std::max(weld_temp_bytes(V), watertight_temp_bytes(T));
+}
+
+cudaError_t indexed_watertight_device(const float *verts, uint32_t V, const uint32_t *idx, uint32_t T, void *temp,
+                                      size_t temp_bytes, int *result, int num_sms, cudaStream_t st) {
+  *result = 0;
+  if (V == 0 || T == 0) return cudaSuccess;
+  if (temp_bytes < indexed_gate_temp_bytes(V, T)) return cudaErrorMemoryAllocation;
+  char *p = static_cast<char *>(temp);
+  unsigned int *misc = reinterpret_cast<unsigned int *>(p);  // bounds [6], error flag [6]
+  uint32_t *wv = reinterpret_cast<uint32_t *>(p + align256(64));
+  uint32_t *tri = reinterpret_cast<uint32_t *>(p + align256(64) + align256(uint64_t(V) * 4));
+  char *rest = p + align256(64) + align256(uint64_t(V) * 4) + align256(uint64_t(T) * 12);
+  const size_t rest_bytes = temp_bytes - size_t(rest - p);
+  const unsigned int init[7] = {~0u, ~0u, ~0u, 0, 0, 0, 0};
+  cudaError_t e = cudaMemcpyAsync(misc, init, sizeof init, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  k_bounds<<<grid_for(V, num_sms), kThreads, 0, st>>>(verts, V, misc);
+  note_launch();
+  unsigned int hb[6];
+  if ((e = cudaMemcpyAsync(hb, misc, sizeof hb, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  float bmin[3], bmax[3];
+  for (int a = 0; a < 3; ++a) {
+    bmin[a] = ordered_to_float(hb[a]);
+    bmax[a] = ordered_to_float(hb[3 + a]);
+  }
+  uint32_t U = 0;
+  if ((e = weld_device(verts, V, weld_cell(bmin, bmax), wv, nullptr, rest, rest_bytes, &U, num_sms, st)) != cudaSuccess)
+    return e;
+  k_map_tris<<<grid_for(uint64_t(T) * 3, num_sms), kThreads, 0, st>>>(idx, uint64_t(T) * 3, V, wv, tri, misc + 6);
+  note_launch();
+  unsigned int bad = 0;
+  if ((e = cudaMemcpyAsync(&bad, misc + 6, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  if (bad) {
+    *result = -2;
+    return cudaSuccess;
+  }
+  uint64_t b = 0, m = 0;
+  if ((e = watertight_device(tri, T, U, rest, rest_bytes, &b, &m, num_sms, st)) != cudaSuccess) return e;
+  *result = (b == 0 && m == 0) ? 1 : 0;
+  return cudaSuccess;
 }
 
 size_t watertight_temp_bytes(uint64_t T) {
