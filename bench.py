@@ -386,6 +386,16 @@ def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, re
     threads = [threading.Thread(target=worker, daemon=True) for _ in range(workers)]
     for th in threads:
         th.start()
+    watching = [True]
+
+    def watch():  # progress on stderr every 10 s
+        while watching[0]:
+            time.sleep(10.0)
+            n_done = sum(1 for r in results if r)
+            stage(f"  serving: {n_done} done, {len(failures)} failed, {len(dropped)} dropped, "
+                  f"{work.qsize()} queued")
+
+    threading.Thread(target=watch, daemon=True).start()
     # warm the server (first-wave allocations) with one small request outside the stream
     v0, f0, _ = base_meshes[0]
     g0 = unit_grid(sdfb, 32)
@@ -402,6 +412,7 @@ def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, re
         work.put(None)
     for th in threads:
         th.join()
+    watching[0] = False
     srv.close()
     if failures:
         print(f"serve_stream: {len(failures)} requests failed, first: {failures[0]}", file=sys.stderr)

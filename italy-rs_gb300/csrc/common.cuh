@@ -244,10 +244,11 @@ constexpr int kFlopsPointPlane = 10;
 
 // ---------------------------------------------------------------------------------------------
 // BVH node (64 bytes): the boxes of both children plus their references, so one 64-byte read
-// yields everything a traversal step needs.
-//   n0 = (c0.lo.x, c0.lo.y, c0.lo.z, c0.hi.x)
-//   n1 = (c0.hi.y, c0.hi.z, c1.lo.x, c1.lo.y)
-//   n2 = (c1.lo.z, c1.hi.x, c1.hi.y, c1.hi.z)
+// yields everything a traversal step needs. A child box is stored as its centre c and half
+// extent e, rounded outward so that [c - e, c + e] contains the box (an empty child has e = -inf):
+//   n0 = (c0.c.x, c0.c.y, c0.c.z, c0.e.x)
+//   n1 = (c0.e.y, c0.e.z, c1.c.x, c1.c.y)
+//   n2 = (c1.c.z, c1.e.x, c1.e.y, c1.e.z)
 //   n3 = (ref0, ref1, cnt0, cnt1) as ints: cnt == 0 -> ref is an inner node index;
 //        cnt > 0 -> leaf of cnt triangles starting at triangle record ref; cnt < 0 -> empty.
 struct Node {
@@ -255,11 +256,13 @@ struct Node {
   int4 n3;
 };
 
-__device__ __forceinline__ float box_dist2(float px, float py, float pz, float lx, float ly, float lz, float hx,
-                                           float hy, float hz) {
-  const float dx = fmaxf(fmaxf(lx - px, px - hx), 0.0f);
-  const float dy = fmaxf(fmaxf(ly - py, py - hy), 0.0f);
-  const float dz = fmaxf(fmaxf(lz - pz, pz - hz), 0.0f);
+// Squared distance from p to the box (centre c, half extent e): per axis max(|p - c| - e, 0), two
+// additions and one maximum (the absolute value is an operand modifier).
+__device__ __forceinline__ float box_dist2(float px, float py, float pz, float cx, float cy, float cz, float ex,
+                                           float ey, float ez) {
+  const float dx = fmaxf(fabsf(px - cx) - ex, 0.0f);
+  const float dy = fmaxf(fabsf(py - cy) - ey, 0.0f);
+  const float dz = fmaxf(fabsf(pz - cz) - ez, 0.0f);
   return dx * dx + dy * dy + dz * dz;
 }
 

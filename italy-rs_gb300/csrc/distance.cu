@@ -166,18 +166,18 @@ __device__ __forceinline__ bool walk(const Node *__restrict__ nodes, const TriRe
       const Node *np = nodes + (e >> 1);
       const float4 n0 = __ldg(&np->n0), n1 = __ldg(&np->n1), n2 = __ldg(&np->n2);
       const int4 n3 = __ldg(&np->n3);
-      float lx0, ly0, lz0, hx0, hy0, hz0;
+      float cx, cy, cz, ex, ey, ez;  // the popped child's box: centre and half extent
       int ref, cnt;
       if (e & 1) {
-        lx0 = n1.z; ly0 = n1.w; lz0 = n2.x; hx0 = n2.y; hy0 = n2.z; hz0 = n2.w;
+        cx = n1.z; cy = n1.w; cz = n2.x; ex = n2.y; ey = n2.z; ez = n2.w;
         ref = n3.y; cnt = n3.w;
       } else {
-        lx0 = n0.x; ly0 = n0.y; lz0 = n0.z; hx0 = n0.w; hy0 = n1.x; hz0 = n1.y;
+        cx = n0.x; cy = n0.y; cz = n0.z; ex = n0.w; ey = n1.x; ez = n1.y;
         ref = n3.x; cnt = n3.z;
       }
       bool want = false;
 #pragma unroll
-      for (int v = 0; v < VPL; ++v) want |= box_dist2(px, py, pz[v], lx0, ly0, lz0, hx0, hy0, hz0) < best[v];
+      for (int v = 0; v < VPL; ++v) want |= box_dist2(px, py, pz[v], cx, cy, cz, ex, ey, ez) < best[v];
       if (COUNT) ws.box_tests += kWarp * VPL;
       if (!__any_sync(kFull, want)) continue;
       if (cnt > 0) test_leaf<VPL, COUNT>(tris, num_tris, ref, cnt, px, py, pz, best, ws);

@@ -279,13 +279,24 @@ __global__ __launch_bounds__(kThreads) void k_refit(int n, const uint32_t *__res
   }
 }
 
+// A child box as centre and half extent (see Node), rounded outward: the half extent is rounded
+// up from both sides of the rounded centre and widened by one part in 2^22, so that the traversal's
+// box distance stays a lower bound of the distance to anything inside.
 __device__ __forceinline__ void put_child(float *box, int which, float4 l, float4 h) {
-  box[which * 6 + 0] = l.x;
-  box[which * 6 + 1] = l.y;
-  box[which * 6 + 2] = l.z;
-  box[which * 6 + 3] = h.x;
-  box[which * 6 + 4] = h.y;
-  box[which * 6 + 5] = h.z;
+  const float lo[3] = {l.x, l.y, l.z}, hi[3] = {h.x, h.y, h.z};
+  const bool empty = !(lo[0] <= hi[0] && lo[1] <= hi[1] && lo[2] <= hi[2]);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (empty) {
+      box[which * 6 + a] = 0.0f;
+      box[which * 6 + 3 + a] = -__int_as_float(0x7f800000);
+      continue;
+    }
+    const float c = __fmul_rn(0.5f, __fadd_rn(lo[a], hi[a]));
+    const float e = fmaxf(__fsub_ru(hi[a], c), __fsub_ru(c, lo[a]));
+    box[which * 6 + a] = c;
+    box[which * 6 + 3 + a] = __fmul_ru(e, 1.0f + 0x1p-22f);
+  }
 }
 
 __device__ __forceinline__ void store_node(Node *nodes, int i, const float *b, int4 refs) {

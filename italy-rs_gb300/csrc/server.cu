@@ -4,9 +4,11 @@
 // time (src/convert/sdf_baker.cpp:150-305). Here a server keeps meshes and their hierarchies
 // resident and runs requests in waves:
 //
-//   * sdfb_mesh_register uploads a mesh, decides its sign mode (weld + watertight gate), caps it
-//     for the winding number when needed, and builds its hierarchy on a registration stream.
-//     Meshes are keyed by a hash of their contents, so a repeat registration is a cache hit.
+//   * sdfb_mesh_register uploads a mesh, decides its sign mode (the weld + watertight gate, on the
+//     device), caps it for the winding number when needed, and builds its hierarchy in one of a
+//     few registration slots (each its own stream and workspace), so registrations from several
+//     threads overlap. Meshes are keyed by a hash of their contents, so a repeat registration is
+//     a cache hit; a thread registering a mesh another thread is building waits for that build.
 //     Resident bytes count against the HBM budget; unreferenced meshes are evicted least
 //     recently used first when a new one needs room.
 //   * sdfb_submit queues a request; the scheduler thread admits queued requests into the next
@@ -27,6 +29,7 @@
 #include <mutex>
 #include <thread>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "api_internal.h"
@@ -37,6 +40,8 @@
 using namespace sdfb;
 
 namespace {
+
+constexpr int kRegSlots = 4;  // meshes registered (uploaded, gated, built) at the same time
 
 double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -120,10 +125,15 @@ bool is_pinned(const void *p) {
 
 struct sdfb_server {
   int device = 0;
-  std::unique_ptr<sdfb_ctx> sched, reg;  // private contexts (streams, workspaces, error text)
+  std::unique_ptr<sdfb_ctx> sched;  // the scheduler's private context (error text, tuned tables)
+  // Registration slots: private contexts (stream, workspace) that build meshes concurrently.
+  std::vector<std::unique_ptr<sdfb_ctx>> regs;
+  std::vector<char> reg_busy;
+  std::unordered_set<uint64_t> building;  // meshes being registered (their first registrant builds)
+  std::condition_variable cv_reg;
   std::vector<std::unique_ptr<Wave>> waves;
   std::thread thread;
-  std::mutex mu, reg_mu;
+  std::mutex mu;
   std::condition_variable cv_work, cv_done;
   bool stop = false;
   std::unordered_map<uint64_t, std::unique_ptr<Resident>> meshes;
@@ -359,7 +369,9 @@ void sdfb_server::run() {
           const uint64_t n = uint64_t(r->grid.nx) * r->grid.ny * r->grid.nz;
           const uint64_t bytes = n * ((r->dist_out ? 4 : 0) + (r->occ_out ? 1 : 0)) + n / 4;
           if (!free_slot->reqs.empty() && (cells + n > wave_cells)) break;
-          if (resident_bytes_used + inflight_bytes + bytes > budget) break;
+          // Room for the outputs: evict unreferenced meshes if needed. When nothing is in flight
+          // the request is admitted even over the budget, so the queue always makes progress.
+          if (resident_bytes_used + inflight_bytes + bytes > budget && !make_room(bytes) && inflight > 0) break;
           pending.pop_front();
           r->t_admit = now_ms();
           free_slot->reqs.push_back(r);
@@ -409,8 +421,12 @@ sdfb_status sdfb_server_create(sdfb_ctx *ctx, const sdfb_server_opts *opts, sdfb
   srv->max_inflight = o.max_inflight > 0 ? o.max_inflight : 64;
   srv->wave_cells = 1ull << (o.wave_voxels_log2 > 10 && o.wave_voxels_log2 < 36 ? o.wave_voxels_log2 : 25);
   srv->sched = make_private_ctx(ctx->device, ctx->num_sms, ctx);
-  srv->reg = make_private_ctx(ctx->device, ctx->num_sms, ctx);
-  if (!srv->sched || !srv->reg) return SDFB_ERR_CUDA;
+  if (!srv->sched) return SDFB_ERR_CUDA;
+  for (int k = 0; k < kRegSlots; ++k) {
+    srv->regs.push_back(make_private_ctx(ctx->device, ctx->num_sms, ctx));
+    if (!srv->regs.back()) return SDFB_ERR_CUDA;
+  }
+  srv->reg_busy.assign(kRegSlots, 0);
   // keep freed device memory in the stream-ordered pool for reuse
   if (cudaDeviceGetDefaultMemPool(&srv->pool, ctx->device) == cudaSuccess) {
     uint64_t keep = ~0ull;
@@ -433,9 +449,19 @@ sdfb_status sdfb_server_create(sdfb_ctx *ctx, const sdfb_server_opts *opts, sdfb
 void sdfb_server_destroy(sdfb_server *srv) {
   if (!srv) return;
   {
+    // requests not yet admitted are cancelled; waves in flight finish
     std::lock_guard<std::mutex> g(srv->mu);
     srv->stop = true;
+    const double t = now_ms();
+    for (Request *r : srv->pending) {
+      r->status = SDFB_ERR_BUSY;
+      r->t_done = t;
+      r->done = true;
+      static_cast<Resident *>(r->res)->refs--;
+    }
+    srv->pending.clear();
   }
+  srv->cv_done.notify_all();
   srv->cv_work.notify_all();
   if (srv->thread.joinable()) srv->thread.join();
   cudaSetDevice(srv->device);
@@ -461,25 +487,45 @@ sdfb_status sdfb_mesh_register(sdfb_server *srv, const float *verts, uint32_t nu
   h = content_hash(idx, size_t(num_tris) * 12, h);
   h = content_hash(&num_verts, 4, h);
   *mesh_id = h;
+  // A cache hit returns at once. Otherwise this thread takes a free registration slot and builds
+  // the mesh, unless another thread is already building the same mesh: then it waits for that
+  // build (a second build would replace a Resident that queued requests may point to).
+  int slot = -1;
   {
-    std::lock_guard<std::mutex> g(srv->mu);
-    auto it = srv->meshes.find(h);
-    if (it != srv->meshes.end()) {
-      it->second->last_use = ++srv->tick;
-      return SDFB_OK;
+    std::unique_lock<std::mutex> lk(srv->mu);
+    for (;;) {
+      auto it = srv->meshes.find(h);
+      if (it != srv->meshes.end()) {
+        it->second->last_use = ++srv->tick;
+        return SDFB_OK;
+      }
+      if (!srv->building.count(h)) {
+        for (size_t k = 0; k < srv->reg_busy.size(); ++k)
+          if (!srv->reg_busy[k]) {
+            slot = static_cast<int>(k);
+            break;
+          }
+        if (slot >= 0) break;
+      }
+      srv->cv_reg.wait(lk);
     }
+    srv->reg_busy[slot] = 1;
+    srv->building.insert(h);
   }
-  std::lock_guard<std::mutex> rg(srv->reg_mu);  // one registration at a time
-  {
-    // Another thread may have registered the same mesh while this one waited for reg_mu; a
-    // second build would replace a Resident that queued requests still point to.
-    std::lock_guard<std::mutex> g(srv->mu);
-    auto it = srv->meshes.find(h);
-    if (it != srv->meshes.end()) {
-      it->second->last_use = ++srv->tick;
-      return SDFB_OK;
+  struct SlotRelease {
+    sdfb_server *s;
+    int slot;
+    uint64_t h;
+    ~SlotRelease() {
+      {
+        std::lock_guard<std::mutex> g(s->mu);
+        s->reg_busy[slot] = 0;
+        s->building.erase(h);
+      }
+      s->cv_reg.notify_all();
     }
-  }
+  } release{srv, slot, h};
+  sdfb_ctx *rc = srv->regs[slot].get();
   cudaSetDevice(srv->device);
   auto r = std::make_unique<Resident>();
   r->id = h;
@@ -493,7 +539,7 @@ sdfb_status sdfb_mesh_register(sdfb_server *srv, const float *verts, uint32_t nu
       return srv->fail(SDFB_ERR_OUT_OF_MEMORY, "mesh does not fit the HBM budget next to in-flight work");
     srv->resident_bytes_used += r->bytes;  // reserved now, released on failure
   }
-  cudaStream_t st = srv->reg->stream;
+  cudaStream_t st = rc->stream;
   auto undo = [&](sdfb_status s, const std::string &m) {
     srv->free_resident(*r, st);
     cudaStreamSynchronize(st);
@@ -511,9 +557,9 @@ sdfb_status sdfb_mesh_register(sdfb_server *srv, const float *verts, uint32_t nu
   std::memset(&auto_opts, 0, sizeof auto_opts);
   auto_opts.sign_mode = SDFB_SIGN_AUTO;
   int sign = kSignParity, watertight = -1;
-  const sdfb_status gs = device_sign(srv->reg.get(), auto_opts, static_cast<const float *>(r->verts.p), num_verts,
+  const sdfb_status gs = device_sign(rc, auto_opts, static_cast<const float *>(r->verts.p), num_verts,
                                      static_cast<const uint32_t *>(r->idx.p), num_tris, st, &sign, &watertight);
-  if (gs != SDFB_OK) return undo(gs, srv->reg->err);
+  if (gs != SDFB_OK) return undo(gs, rc->err);
   r->sign = sign;
   r->watertight = watertight;
   CapBuild caps;
@@ -555,11 +601,11 @@ sdfb_status sdfb_mesh_register(sdfb_server *srv, const float *verts, uint32_t nu
   p.pV = r->pV;
   p.cT = r->cT;
   p.grid.nx = p.grid.ny = p.grid.nz = 256;  // leaf size is tuned for a typical grid
-  const sdfb_status s = build_resident(srv->reg.get(), srv->reg->ws, st, p, r->bvh.p, r->tree, r->caps.p, r->cap_tree);
-  if (s != SDFB_OK) return undo(s, srv->reg->err);
+  const sdfb_status s = build_resident(rc, rc->ws, st, p, r->bvh.p, r->tree, r->caps.p, r->cap_tree);
+  if (s != SDFB_OK) return undo(s, rc->err);
   std::lock_guard<std::mutex> g(srv->mu);
   r->last_use = ++srv->tick;
-  srv->meshes.emplace(h, std::move(r));  // registrations are serialised by reg_mu: h is new
+  srv->meshes.emplace(h, std::move(r));  // h was in `building`, so no other thread inserted it
   return SDFB_OK;
 }
 

@@ -90,13 +90,15 @@ def test_pinned_outputs(ctx):
 
 
 def test_concurrent_registration_of_the_same_mesh(ctx):
-    """Many threads register the same few meshes at once and submit right away (the serving
-    stream's repeats): each mesh is built once, and every result equals the plain bake."""
+    """Many threads register a few meshes at once and submit right away (the serving stream's
+    repeats): registrations of different meshes overlap in the registration slots, each mesh is
+    built once, and every result equals the plain bake."""
     import threading
 
     import sdfb
     from sdfb import meshgen as mg
-    meshes = [mg.displaced_icosphere(4, 0.3, 21), mg.displaced_torus(60, 20, 0.27, 0.1, 22)]
+    meshes = [mg.displaced_icosphere(4, 0.3, 21), mg.displaced_torus(60, 20, 0.27, 0.1, 22),
+              mg.displaced_icosphere(3, 0.35, 23), mg.displaced_torus(40, 16, 0.3, 0.08, 24)]
     n = 40
     g = sdfb.make_grid((-0.5,) * 3, 1.0 / n, (n, n, n))
     ref = [ctx.bake(v, f, g, sdfb.make_opts()) for v, f in meshes]
@@ -106,13 +108,13 @@ def test_concurrent_registration_of_the_same_mesh(ctx):
 
         def worker(k):
             try:
-                v, f = meshes[k % 2]
+                v, f = meshes[k % 4]
                 start.wait()
                 mid = srv.register(v, f)
                 d = np.empty(g.shape, np.float32)
                 o = np.empty(g.shape, np.uint8)
                 done, info = srv.poll(srv.submit(mid, g, d, o), 60000)
-                results.append((k % 2, done, info["status"], d, o))
+                results.append((k % 4, done, info["status"], d, o))
             except Exception as e:  # reported below
                 errors.append(repr(e))
 
@@ -126,3 +128,44 @@ def test_concurrent_registration_of_the_same_mesh(ctx):
     for m, done, status, d, o in results:
         assert done and status == 0
         assert np.array_equal(d, ref[m][0]) and np.array_equal(o, ref[m][1])
+
+
+def test_admission_evicts_and_always_progresses(ctx):
+    """Registered meshes may fill the budget; admitting a request then evicts unreferenced meshes
+    for its outputs, and a request larger than what is left is still admitted when nothing else
+    is in flight."""
+    import sdfb
+    from sdfb import meshgen as mg
+    ms = [mg.displaced_icosphere(4, 0.3, 40 + s) for s in range(2)]
+    per_mesh = 5120 * 160
+    with sdfb.Server(ctx, hbm_budget_bytes=int(per_mesh * 2.2)) as srv:
+        a = srv.register(*ms[0])
+        b = srv.register(*ms[1])
+        for n in (40, 96):  # 40^3 outputs need an eviction; 96^3 outputs exceed the whole budget
+            g = sdfb.make_grid((-0.5,) * 3, 1.0 / n, (n, n, n))
+            d = np.empty(g.shape, np.float32)
+            o = np.empty(g.shape, np.uint8)
+            done, info = srv.poll(srv.submit(b, g, d, o), 60000)
+            assert done and info["status"] == 0
+            d1, o1 = ctx.bake(*ms[1], g, sdfb.make_opts())
+            assert np.array_equal(d, d1) and np.array_equal(o, o1)
+        del a
+
+
+def test_close_with_requests_queued(ctx):
+    """Closing the server cancels what is still queued and returns."""
+    import threading
+
+    import sdfb
+    from sdfb import meshgen as mg
+    v, f = mg.displaced_icosphere(4, 0.3, 50)
+    srv = sdfb.Server(ctx, max_inflight=1, wave_voxels_log2=12)
+    mid = srv.register(v, f)
+    g = sdfb.make_grid((-0.5,) * 3, 1.0 / 64, (64, 64, 64))
+    bufs = [(np.empty(g.shape, np.float32), np.empty(g.shape, np.uint8)) for _ in range(20)]
+    for d, o in bufs:
+        srv.submit(mid, g, d, o)
+    t = threading.Thread(target=srv.close, daemon=True)
+    t.start()
+    t.join(60)
+    assert not t.is_alive()
