@@ -35,8 +35,12 @@
 namespace sdfb {
 namespace {
 
+// Pass A runs warps independently, so small blocks let the register file hold as many warps as it
+// can (the 4x4x8 and 8x4x4 tiles need about 104 registers: 18 warps per SM in blocks of 2 warps,
+// 16 in blocks of 8). Pass B's block shares one tile: 8 warps.
+constexpr int kThreadsA = 64;
+constexpr int kWarpsPerBlockA = kThreadsA / kWarp;
 constexpr int kThreads = 256;
-constexpr int kWarpsPerBlock = kThreads / kWarp;
 constexpr int kSplitBits = 5;  // pass B: 32 subtrees per deferred tile
 constexpr float kInf = __builtin_huge_valf();
 
@@ -285,7 +289,7 @@ __device__ __forceinline__ void flush_stats(const DistanceArgs &a, const WalkSta
 
 // Pass A: one warp per tile, tiles from a global counter; tiles over the step budget are deferred.
 template <int TX, int TY, int TZ, int STACK, bool COUNT>
-__global__ __launch_bounds__(kThreads) void k_distance(DistanceArgs a) {
+__global__ __launch_bounds__(kThreadsA) void k_distance(DistanceArgs a) {
   using Cells = TileCells<TX, TY, TZ>;
   constexpr int VPL = Cells::VPL;
   const int lane = threadIdx.x & 31;
@@ -432,25 +436,25 @@ __global__ __launch_bounds__(kThreads) void k_distance_deferred(DistanceArgs a) 
 }
 
 template <typename K>
-int blocks_per_sm(K kernel) {
+int blocks_per_sm(K kernel, int threads) {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
   return per_sm > 0 ? per_sm : 1;
 }
 
 template <int I, int STACK, bool COUNT>
 cudaError_t launch_shape(const DistanceArgs &a, int num_sms, cudaStream_t st) {
   constexpr Shape s = kShapes[I];
-  static const int per_sm = blocks_per_sm(k_distance<s.tx, s.ty, s.tz, STACK, COUNT>);
-  static const int per_sm_b = blocks_per_sm(k_distance_deferred<s.tx, s.ty, s.tz, STACK, COUNT>);
+  static const int per_sm = blocks_per_sm(k_distance<s.tx, s.ty, s.tz, STACK, COUNT>, kThreadsA);
+  static const int per_sm_b = blocks_per_sm(k_distance_deferred<s.tx, s.ty, s.tz, STACK, COUNT>, kThreads);
   const unsigned long long warps_needed = a.batch.total_tiles;
   unsigned long long blocks = static_cast<unsigned long long>(num_sms) * per_sm;
-  blocks = std::min<unsigned long long>(blocks, (warps_needed + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  blocks = std::min<unsigned long long>(blocks, (warps_needed + kWarpsPerBlockA - 1) / kWarpsPerBlockA);
   if (blocks < 1) blocks = 1;
   cudaError_t e = cudaMemsetAsync(a.tile_counter, 0, sizeof(unsigned long long), st);
   if (e == cudaSuccess && a.defer_list) e = cudaMemsetAsync(a.defer_counters, 0, 2 * sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
-  k_distance<s.tx, s.ty, s.tz, STACK, COUNT><<<static_cast<unsigned>(blocks), kThreads, 0, st>>>(a);
+  k_distance<s.tx, s.ty, s.tz, STACK, COUNT><<<static_cast<unsigned>(blocks), kThreadsA, 0, st>>>(a);
   note_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess || !a.defer_list || a.step_budget <= 0) return e;
