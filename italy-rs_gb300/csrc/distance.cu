@@ -42,10 +42,6 @@ constexpr int kThreadsA = 64;
 constexpr int kWarpsPerBlockA = kThreadsA / kWarp;
 constexpr int kThreads = 256;
 constexpr int kSplitBits = 5;  // pass B: 32 subtrees per deferred tile
-// Tiles are numbered in bricks of 2x2x2 tiles and a warp takes a whole brick at a time, so the
-// tiles one warp walks in a row are neighbours and find the same nodes and triangles in L1.
-constexpr bool kBricks = true;
-constexpr int kChunk = kBricks ? 8 : 1;
 constexpr float kInf = __builtin_huge_valf();
 
 struct Shape {
@@ -78,22 +74,10 @@ struct TileCells {
     g = M->g;
     const unsigned long long local = tile - B.tile_starts[mesh];
     const int tiles_x = (g.nx + TX - 1) / TX, tiles_y = (g.ny + TY - 1) / TY;
-    int tx, ty, tz;
-    if (kBricks) {  // brick (x fastest), then the tile within the brick (x, y, z bits); tiles past
-                    // the grid's edge have no active cell
-      const int bricks_x = (tiles_x + 1) >> 1, bricks_y = (tiles_y + 1) >> 1;
-      const unsigned long long brick = local >> 3;
-      const int sub = static_cast<int>(local & 7);
-      const unsigned long long rest = brick / bricks_x;
-      tx = 2 * static_cast<int>(brick % bricks_x) + (sub & 1);
-      ty = 2 * static_cast<int>(rest % bricks_y) + ((sub >> 1) & 1);
-      tz = 2 * static_cast<int>(rest / bricks_y) + (sub >> 2);
-    } else {
-      tx = static_cast<int>(local % tiles_x);
-      const unsigned long long rest = local / tiles_x;
-      ty = static_cast<int>(rest % tiles_y);
-      tz = static_cast<int>(rest / tiles_y);
-    }
+    const int tx = static_cast<int>(local % tiles_x);
+    const unsigned long long rest = local / tiles_x;
+    const int ty = static_cast<int>(rest % tiles_y);
+    const int tz = static_cast<int>(rest / tiles_y);
     vx = tx * TX + lane % TX;
     vy = ty * TY + (lane / TX) % TY;
     vz0 = tz * TZ + lane / kLayer;
@@ -303,8 +287,8 @@ __device__ __forceinline__ void flush_stats(const DistanceArgs &a, const WalkSta
   }
 }
 
-// Pass A: one warp per tile, bricks of tiles from a global counter; a tile still walking in the
-// pass's tail is deferred to pass B.
+// Pass A: one warp per tile, tiles from a global counter; a tile still walking in the pass's tail
+// is deferred to pass B.
 template <int TX, int TY, int TZ, int STACK, bool COUNT>
 __global__ __launch_bounds__(kThreadsA) void k_distance(DistanceArgs a) {
   using Cells = TileCells<TX, TY, TZ>;
@@ -317,38 +301,34 @@ __global__ __launch_bounds__(kThreadsA) void k_distance(DistanceArgs a) {
   const TailCheck never{nullptr, 0, 0};
 
   for (;;) {
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(a.tile_counter, static_cast<unsigned long long>(kChunk));
-    base = __shfl_sync(kFull, base, 0);
-    if (base >= B.total_tiles) break;
-    const unsigned long long stop = base + static_cast<unsigned long long>(kChunk);
-    const unsigned long long end = stop < B.total_tiles ? stop : B.total_tiles;
-    for (unsigned long long tile = base; tile < end; ++tile) {
-      Cells c;
-      c.locate(B, tile, lane);
-      const MeshRec &M = *c.M;
-      float best[VPL];
+    unsigned long long tile = 0;
+    if (lane == 0) tile = atomicAdd(a.tile_counter, 1ull);
+    tile = __shfl_sync(kFull, tile, 0);
+    if (tile >= B.total_tiles) break;
+    Cells c;
+    c.locate(B, tile, lane);
+    const MeshRec &M = *c.M;
+    float best[VPL];
 #pragma unroll
-      for (int v = 0; v < VPL; ++v) best[v] = c.active[v] ? kInf : -1.0f;
-      bool done = walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, M.root, tail, lane, c.px, c.py,
-                                          c.pz, c.active, best, ws);
-      if (!done) {
-        unsigned long long slot = 0;
-        if (lane == 0) slot = atomicAdd(a.defer_counters, 1ull);
-        slot = __shfl_sync(kFull, slot, 0);
-        if (slot < a.defer_capacity) {
-          if (lane == 0) a.defer_list[slot] = tile;
+    for (int v = 0; v < VPL; ++v) best[v] = c.active[v] ? kInf : -1.0f;
+    bool done = walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, M.root, tail, lane, c.px, c.py,
+                                        c.pz, c.active, best, ws);
+    if (!done) {
+      unsigned long long slot = 0;
+      if (lane == 0) slot = atomicAdd(a.defer_counters, 1ull);
+      slot = __shfl_sync(kFull, slot, 0);
+      if (slot < a.defer_capacity) {
+        if (lane == 0) a.defer_list[slot] = tile;
 #pragma unroll
-          for (int v = 0; v < VPL; ++v)
-            if (c.active[v]) M.dist[c.cell(v)] = best[v];  // the bounds pass B starts from
-          continue;
-        }
-        // The list is full: finish the tile here, from the bounds found so far.
-        walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, M.root, never, lane, c.px, c.py, c.pz,
-                                c.active, best, ws);
+        for (int v = 0; v < VPL; ++v)
+          if (c.active[v]) M.dist[c.cell(v)] = best[v];  // the bounds pass B starts from
+        continue;
       }
-      store_cells<TX, TY, TZ>(a, c, best);
+      // The list is full: finish the tile here, from the bounds found so far.
+      walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, M.root, never, lane, c.px, c.py, c.pz,
+                              c.active, best, ws);
     }
+    store_cells<TX, TY, TZ>(a, c, best);
   }
   flush_stats<COUNT>(a, ws, lane);
 }
@@ -468,7 +448,7 @@ cudaError_t launch_shape(const DistanceArgs &a, int num_sms, cudaStream_t st) {
   constexpr Shape s = kShapes[I];
   static const int per_sm = blocks_per_sm(k_distance<s.tx, s.ty, s.tz, STACK, COUNT>, kThreadsA);
   static const int per_sm_b = blocks_per_sm(k_distance_deferred<s.tx, s.ty, s.tz, STACK, COUNT>, kThreads);
-  const unsigned long long warps_needed = (a.batch.total_tiles + kChunk - 1) / kChunk;
+  const unsigned long long warps_needed = a.batch.total_tiles;
   unsigned long long blocks = static_cast<unsigned long long>(num_sms) * per_sm;
   blocks = std::min<unsigned long long>(blocks, (warps_needed + kWarpsPerBlockA - 1) / kWarpsPerBlockA);
   if (blocks < 1) blocks = 1;
@@ -514,9 +494,7 @@ void tile_shape(int id, int &tx, int &ty, int &tz) {
 uint64_t tiles_for(const GridDev &g, int id) {
   int tx, ty, tz;
   tile_shape(id, tx, ty, tz);
-  const uint64_t nx = (g.nx + tx - 1) / tx, ny = (g.ny + ty - 1) / ty, nz = (g.nz + tz - 1) / tz;
-  if (kBricks) return 8 * ((nx + 1) / 2) * ((ny + 1) / 2) * ((nz + 1) / 2);  // whole bricks
-  return nx * ny * nz;
+  return uint64_t((g.nx + tx - 1) / tx) * uint64_t((g.ny + ty - 1) / ty) * uint64_t((g.nz + tz - 1) / tz);
 }
 
 uint64_t defer_capacity_for(uint64_t total_tiles) {
