@@ -184,7 +184,8 @@ class ClockSampler:
 
 
 def cpu_bake(orc, ref, v, i, n):
-    """One CPU bake of mesh (v, i) on the n^3 unit grid; returns seconds."""
+    """One CPU bake of mesh (v, i) on the n^3 unit grid; returns (seconds, FP64 unsigned distance,
+    exact parity sign)."""
     from oracle.oracle import soup_of
     origin, voxel, dims = (-0.5, -0.5, -0.5), 1.0 / n, (n, n, n)
     soup = soup_of(v, i) if ref is not None else None
@@ -196,7 +197,7 @@ def cpu_bake(orc, ref, v, i, n):
     d = orc.distance(v, i, origin, voxel, dims)
     s = orc.sign_parity(v, i, origin, voxel, dims, axis=2)
     (d * s).astype("float32")
-    return time.perf_counter() - t0
+    return time.perf_counter() - t0, d, s
 
 
 def cpu_tools():
@@ -214,9 +215,10 @@ def cpu_tools():
     return orc, ref, kind
 
 
-def cpu_sample(meshes, budget_s, seed, orc, ref):
-    """CPU bakes of the workload's meshes in a seeded order until about budget_s seconds.
-    Returns (voxels, seconds, meshes used)."""
+def cpu_sample(meshes, budget_s, seed, orc, ref, check=None):
+    """CPU bakes of the workload's meshes in a seeded order until about budget_s seconds; check(k,
+    d, s), when given, sees each baked mesh's result (outside the timing). Returns (voxels,
+    seconds, meshes used)."""
     import numpy as np
     order = np.random.default_rng(seed).permutation(len(meshes))
     vox, secs, used = 0, 0.0, 0
@@ -225,18 +227,43 @@ def cpu_sample(meshes, budget_s, seed, orc, ref):
         est = n ** 3 * 1.5e-6 * max(1.0, math.log2(max(len(i), 2)) / 17)  # skip bakes far over budget
         if used and secs + est > budget_s * 1.5:
             continue
-        secs += cpu_bake(orc, ref, v, i, n)
+        dt, d, sg = cpu_bake(orc, ref, v, i, n)
+        secs += dt
         vox += n ** 3
         used += 1
+        if check is not None:
+            check(k, d, sg)
         if secs >= budget_s:
             break
     return vox, secs, used
 
 
-def cpu_baseline(meshes, budget_s=20.0, seed=0):
+def cpu_baseline(meshes, budget_s=20.0, seed=0, gpu_grids=None):
+    """The CPU baseline; given the GPU's signed grids of the same meshes (gpu_grids[k]) it also
+    reports their error against the CPU bake of every sampled mesh, on every cell."""
+    import numpy as np
     orc, ref, kind = cpu_tools()
-    vox, secs, used = cpu_sample(meshes, budget_s, seed, orc, ref)
-    return {"value": vox / secs, "unit": "voxels/s", "cores": orc.threads(), "kind": kind,
+    stats = {"max": 0.0, "sq": 0.0, "cells": 0, "sign_far_mismatch": 0, "meshes": 0}
+
+    def check(k, d, sg):
+        n = meshes[k][2]
+        got = np.asarray(gpu_grids[k], np.float32).reshape(-1)
+        err = np.abs(np.abs(got.astype(np.float64)) - d) / np.sqrt(3.0)
+        stats["max"] = max(stats["max"], float(err.max()))
+        stats["sq"] += float((err ** 2).sum())
+        stats["cells"] += err.size
+        far = d > 1.0 / n
+        stats["sign_far_mismatch"] += int(np.count_nonzero((got[far] < 0) != (sg[far] < 0)))
+        stats["meshes"] += 1
+
+    vox, secs, used = cpu_sample(meshes, budget_s, seed, orc, ref, check if gpu_grids is not None else None)
+    precision = None
+    if gpu_grids is not None and stats["cells"]:
+        precision = {"max_err_over_diag": stats["max"], "rms_err_over_diag": math.sqrt(stats["sq"] / stats["cells"]),
+                     "cells": stats["cells"], "meshes": stats["meshes"],
+                     "sign_mismatches_outside_1_voxel": stats["sign_far_mismatch"],
+                     "reference": "FP64 oracle distance and exact parity on every cell of the sampled meshes"}
+    return {"value": vox / secs, "unit": "voxels/s", "cores": orc.threads(), "kind": kind, "precision": precision,
             "sample": f"{used} of the workload's meshes in seeded order, {vox} voxels, {secs:.1f} s "
                       f"(occupancy: {'the reference triBoxOverlap' if kind == 'reference' else 'oracle port'}, 1 thread;"
                       f" FP64 distance + exact parity: {orc.threads()} threads)"}
@@ -623,27 +650,15 @@ def main(argv=None):
                 "peak_source": "cuBLAS SGEMM 8192^3 FP32 (TF32 off), best of 5, measured in this run",
                 "algorithmic_bytes_per_launch": total_cells * 4}
 
-    # ---- precision against FP64 on a seeded sample of every mesh ----
-    from oracle.oracle import Oracle
-    orc = Oracle()
-    rng = np.random.default_rng(0)
-    errs = []
-    for k, (v, i, n) in enumerate(meshes):
-        samp = np.sort(rng.choice(n ** 3, min(n ** 3, 2000), replace=False)).astype(np.int64)
-        d64 = orc.distance(v, i, (-0.5,) * 3, 1.0 / n, (n, n, n), samples=samp)
-        got = np.abs(hd[k].reshape(-1)[samp].astype(np.float64))
-        errs.append(np.abs(got - d64) / (np.sqrt(3.0)))
-    err = np.concatenate(errs)
-    stage(f"precision: max {err.max():.3g} x diag")
-
     served = None
     if not args.no_serve and args.workload == "batch64" and world == 1:
         served, reqs = serve_stream(sdfb, ctx, torch, meshes, args.serve_seconds)
         stage(f"served: {served['completed']}/{served['requests']} in {served['seconds']:.1f} s")
         served["plain"] = plain_stream(sdfb, ctx, meshes, reqs, min(10.0, args.serve_seconds))
         stage("plain stream done")
-    cpu = None if args.no_cpu_baseline else cpu_baseline(meshes)
-    stage("CPU baseline done")
+    cpu = None if args.no_cpu_baseline else cpu_baseline(meshes, gpu_grids=hd)
+    precision = cpu.pop("precision") if cpu else None
+    stage("CPU baseline done" + (f": max error {precision['max_err_over_diag']:.3g} x diag" if precision else ""))
     line = {
         "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sum(step_ms) / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -661,8 +676,7 @@ def main(argv=None):
         "clocks": clk,
         "gpu_launches": int(sum(launches)),
         "graph_replayed_steps": int(sum(replayed)),
-        "precision": {"max_err_over_diag": float(err.max()), "rms_err_over_diag": float(np.sqrt((err ** 2).mean())),
-                      "samples": int(len(err)), "reference": "FP64 oracle"},
+        "precision": precision,
         "served": served,
         "single_mesh": single,
     }

@@ -1,13 +1,13 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
 * ``build_oracle()`` compiles this project's C restatement ``oracle/sdf_oracle.c`` into
-  ``oracle/_build/liboracle.so``. It runs here and on the GPU machine.
+  ``oracle/_build/liboracle.so``. It runs on every machine that runs the tests.
 * ``build_ref()`` compiles the reference's own CPU sources for the bake path -- the
   triangle/box test header, ``voxelize.cpp``, ``mesh_weld.cpp`` and ``mesh_validate.cpp`` --
   where they lie in the reference tree, against the small glm stand-in in
   ``oracle/glm_shim``, together with ``oracle/ref_driver.cpp``, into
   ``oracle/_ref/libitaly_ref.so``. It needs the reference tree (``ITALY_REF_ROOT``, default
-  ``/root/reference``) and is skipped when that tree is absent (the GPU machine).
+  ``/root/reference``) and is skipped when that tree is absent.
 
 Both use ``-ffp-contract=off``: FP32 occupancy must round exactly as the reference does.
 """

@@ -1,7 +1,8 @@
 """ctypes front end of the CPU oracle (test infrastructure only).
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline / reference legs use this
-module, and only as the checker or the timed CPU baseline; the product library never imports it.
+module, and only as the reference for comparisons or the timed CPU baseline; the product library
+never imports it.
 
 ``Oracle`` wraps ``oracle/_build/liboracle.so`` (this project's restatement, see sdf_oracle.c).
 ``Reference`` wraps ``oracle/_ref/libitaly_ref.so``, the reference's own CPU sources compiled
