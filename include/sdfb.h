@@ -95,8 +95,8 @@ typedef struct sdfb_stats {
   int32_t tile_used;
   int32_t stack_used;
   double ms_total;         /* first to last event on the device */
-  double ms_prepare;       /* validation, triangle layout, bounds */
-  double ms_build;         /* Morton codes, sort, hierarchy, refit */
+  double ms_prepare;       /* upload of the batch tables and counter reset */
+  double ms_build;         /* triangle records, Morton codes, sort, hierarchy, refit, layout */
   double ms_occupancy;
   double ms_sign;          /* parity crossings or winding-number band */
   double ms_distance;      /* nearest-triangle traversal (+ fused sign) */

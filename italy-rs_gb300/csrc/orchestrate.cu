@@ -432,6 +432,7 @@ sdfb_status enqueue_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, std::ve
     return cudaEventRecordWithFlags(e, st, capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
   };
   auto enqueue = [&]() -> sdfb_status {
+    CK(rec(ws.ev[6]));
     CK(cudaMemcpyAsync(ws.batch_buf.p, ws.staging.p, L.bytes, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(ws.misc.p, 0, 256, st));
     CK(rec(ws.ev[0]));
@@ -533,14 +534,16 @@ sdfb_status finish_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, const Ba
     sv.leaf_size_used = S.leaf0;
     sv.tile_used = S.tile_id + 1;
     sv.stack_used = S.stack;
-    float ms_b = 0, ms_o = 0, ms_s = 0, ms_d = 0, ms_g = 0, tot = 0;
+    float ms_p = 0, ms_b = 0, ms_o = 0, ms_s = 0, ms_d = 0, ms_g = 0, tot = 0;
+    cudaEventElapsedTime(&ms_p, ws.ev[6], ws.ev[0]);
     cudaEventElapsedTime(&ms_b, ws.ev[0], ws.ev[1]);
     cudaEventElapsedTime(&ms_o, ws.ev[1], ws.ev[2]);
     cudaEventElapsedTime(&ms_s, ws.ev[2], ws.ev[3]);
     cudaEventElapsedTime(&ms_d, ws.ev[3], ws.ev[4]);
     cudaEventElapsedTime(&ms_g, ws.ev[4], ws.ev[5]);
-    cudaEventElapsedTime(&tot, ws.ev[0], ws.ev[5]);
+    cudaEventElapsedTime(&tot, ws.ev[6], ws.ev[5]);
     sv.ms_total = tot;
+    sv.ms_prepare = ms_p;
     sv.ms_build = ms_b;
     sv.ms_occupancy = ms_o;
     sv.ms_sign = ms_s + ms_g;
