@@ -299,6 +299,17 @@ def run_reference(args, rank, world):
 # GPU arm
 
 
+def hbm_peak_gbs():
+    """The measured copy bandwidth of this GPU model (MEASURED_PEAKS.json beside this file), else
+    the fallback figure."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (copy)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback 6.8 TB/s"
+
+
 def sgemm_peak(torch) -> float:
     """FP32 CUDA-core peak measured as cuBLAS SGEMM (TF32 off), TFLOP/s, best of 5."""
     torch.backends.cuda.matmul.allow_tf32 = False
@@ -649,6 +660,13 @@ def main(argv=None):
                 "plane_tests": int(cst.plane_tests), "tiles_deferred": int(cst.tiles_deferred), "kernel_ms": mean_dist_ms,
                 "peak_source": "cuBLAS SGEMM 8192^3 FP32 (TF32 off), best of 5, measured in this run",
                 "algorithmic_bytes_per_launch": total_cells * 4}
+    # the memory side beside it: distance writes plus one read of every mesh's hierarchy
+    hbm_peak, hbm_src = hbm_peak_gbs()
+    bvh_bytes = sum(len(i) * (64 + 64) for _, i, _ in meshes)  # triangle records + nodes
+    moved = total_cells * 4 + bvh_bytes
+    roofline["hbm"] = {"bytes_per_launch": moved, "achieved_gbs": moved / (mean_dist_ms * 1e-3) / 1e9,
+                       "peak_gbs": hbm_peak, "frac": moved / (mean_dist_ms * 1e-3) / 1e9 / hbm_peak,
+                       "peak_source": hbm_src}
 
     served = None
     if not args.no_serve and args.workload == "batch64" and world == 1:
