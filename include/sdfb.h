@@ -319,7 +319,7 @@ sdfb_status sdfb_submit(sdfb_server *srv, uint64_t mesh_id, const sdfb_grid_desc
  * with its outcome in info (optional). A finished request is forgotten after it is reported. */
 sdfb_status sdfb_poll(sdfb_server *srv, uint64_t request_id, int32_t timeout_ms, int32_t *done,
                       sdfb_request_info *info);
-/* Text of the server's last error. */
+/* Text of the server's last error (valid in the calling thread until its next call here). */
 const char *sdfb_server_last_error(const sdfb_server *srv);
 
 /* ---- occupancy without allocation (no counterpart in the reference) ---------------------- */

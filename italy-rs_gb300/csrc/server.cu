@@ -475,7 +475,16 @@ void sdfb_server_destroy(sdfb_server *srv) {
   delete srv;
 }
 
-const char *sdfb_server_last_error(const sdfb_server *srv) { return srv ? srv->err.c_str() : "null server"; }
+const char *sdfb_server_last_error(const sdfb_server *srv) {
+  if (!srv) return "null server";
+  // a copy per calling thread: other threads may set a new error meanwhile
+  thread_local std::string copy;
+  {
+    std::lock_guard<std::mutex> g(const_cast<sdfb_server *>(srv)->err_mu);
+    copy = srv->err;
+  }
+  return copy.c_str();
+}
 
 sdfb_status sdfb_mesh_register(sdfb_server *srv, const float *verts, uint32_t num_verts, const uint32_t *idx,
                                uint32_t num_tris, uint64_t *mesh_id) {
