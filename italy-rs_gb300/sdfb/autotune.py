@@ -36,10 +36,21 @@ STACKS = (32, 64)
 BUDGETS = (-1, 512, 1024, 2048, 4096)
 START = (4, 3, 64, 1024)  # leaf, tile id (1-based), stack, step budget: the built-in defaults
 
-# (icosphere level, grid edge): 1,280 .. 327,680 triangles on 64^3 .. 512^3 grids
+# (mesh, grid edge): displaced icospheres of levels 3..7 (1,280 .. 327,680 triangles) on 64^3 .. 512^3
+# grids, and displaced tori of 131,072 and 1,048,576 triangles (thin tubes; the largest meshes a
+# batch holds) on 128^3 and 256^3 grids
 SWEEP = [(3, 64), (3, 128), (3, 256), (4, 64), (4, 128), (4, 256), (5, 128), (5, 256), (5, 512),
-         (6, 128), (6, 256), (6, 512), (7, 128), (7, 256), (7, 512)]
+         (6, 128), (6, 256), (6, 512), (7, 128), (7, 256), (7, 512),
+         ("torus128k", 128), ("torus128k", 256), ("torus1m", 128), ("torus1m", 256)]
 QUICK = [(4, 128), (6, 256), (7, 256)]
+TORI = {"torus128k": (512, 128), "torus1m": (1024, 512)}  # nu x nv quads, 2 nu nv triangles
+
+
+def sweep_mesh(meshgen, key):
+    if key in TORI:
+        nu, nv = TORI[key]
+        return meshgen.displaced_torus(nu, nv, 0.3, 0.1, 90 + nu)
+    return meshgen.displaced_icosphere(key, 0.4, 100 + key)
 
 
 def bucket_tris(t: int) -> int:
@@ -144,7 +155,7 @@ def main(argv=None):
     meshes = {}
     for level, n in (QUICK if args.quick else SWEEP):
         if level not in meshes:
-            meshes[level] = meshgen.displaced_icosphere(level, 0.4, 100 + level)
+            meshes[level] = sweep_mesh(meshgen, level)
         v, f = meshes[level]
         grid = sdfb.make_grid((-0.5, -0.5, -0.5), 1.0 / n, (n, n, n))
         dv = torch.from_numpy(np.ascontiguousarray(v, np.float32)).cuda()
@@ -161,7 +172,7 @@ def main(argv=None):
     table = fill_table(measured)
     header = [f"written by italy-rs_gb300/sdfb/autotune.py{' --quick' if args.quick else ''} on "
               f"{torch.cuda.get_device_name(0)}, {datetime.date.today().isoformat()}",
-              f"{len(measured)} buckets measured (displaced icospheres, parity sign, median of {args.reps}); "
+              f"{len(measured)} buckets measured (displaced icospheres and tori, parity sign, median of {args.reps}); "
               f"the rest filled from the nearest"]
     write_table(args.out, table, measured, times, header)
     print(f"wrote {args.out}")
