@@ -18,7 +18,8 @@ Workloads (seeded synthetic meshes generated in-process; no dataset is involved)
 Also reported: ``served`` -- a Poisson stream (200 requests/s for --serve-seconds, default 60) of
 meshes drawn as in batch64 (30% of requests repeat an earlier mesh, the rest bring a new one) fed
 to the serving loop under a 150 GB budget, with voxels/s and p50/p99 latency (arrival to
-completion), beside the same stream's first seconds served by plain per-request bakes;
+completion), beside the same stream's first seconds served by plain per-request bakes, and
+(``served.light``) a 60 requests/s stream for up to 30 s, a load one GPU keeps up with;
 ``single_mesh`` -- the 256^3 displaced-sphere bake; ``roofline`` of the distance kernel (FP32
 CUDA-core work: algorithmic flops per launch from the counting build of the same kernel over the
 kernel's CUDA-event time, against a cuBLAS SGEMM measured in this run); ``cpu_baseline`` -- the
@@ -674,6 +675,11 @@ def main(argv=None):
         stage(f"served: {served['completed']}/{served['requests']} in {served['seconds']:.1f} s")
         served["plain"] = plain_stream(sdfb, ctx, meshes, reqs, min(10.0, args.serve_seconds))
         stage("plain stream done")
+        # the same kind of stream at a rate one GPU keeps up with, for latency without a queue
+        light, _ = serve_stream(sdfb, ctx, torch, meshes, min(30.0, args.serve_seconds), seed=78, rate=60.0)
+        served["light"] = {k: light[k] for k in ("requests", "completed", "voxels_per_s", "p50_ms", "p99_ms",
+                                                 "mean_ms", "rate_per_s")}
+        stage(f"light stream: p50 {light['p50_ms']:.0f} ms, p99 {light['p99_ms']:.0f} ms")
     cpu = None if args.no_cpu_baseline else cpu_baseline(meshes, gpu_grids=hd)
     precision = cpu.pop("precision") if cpu else None
     stage("CPU baseline done" + (f": max error {precision['max_err_over_diag']:.3g} x diag" if precision else ""))
