@@ -37,7 +37,8 @@ struct PinBuf {
 // A mesh hierarchy resident in device memory (built once, reused by later bakes).
 struct ResidentBvh {
   const sdfb::Node *nodes = nullptr;
-  const sdfb::TriRec *tris = nullptr;
+  const sdfb::DistTri *dtris = nullptr;  // distance hierarchy
+  const sdfb::TriRec *tris = nullptr;    // winding-number hierarchy
   const uint32_t *leaf_order = nullptr;
   const float *node_area = nullptr;
   int num_nodes = 0, num_inner = 0, num_tris = 0, root = 0;
@@ -177,7 +178,7 @@ sdfb_status run_batch(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &mes
                       bool use_graph, sdfb_stats *stats);
 // Builds the hierarchy of one mesh (and of its caps when cT > 0) into `mem` / `cap_mem`, which
 // must hold resident_bytes(T) / resident_bytes(cT, true). Enqueued on st with ws's temporaries.
-size_t resident_bytes(uint64_t tris, bool with_areas = false);
+size_t resident_bytes(uint64_t tris, bool winding = false);
 sdfb_status build_resident(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, const PlanMesh &mesh, void *mem,
                            ResidentBvh &out, void *cap_mem, ResidentBvh &cap_out);
 

@@ -15,6 +15,7 @@ enum DevErr : uint32_t {
   kErrCrossingOverflow = 8u,  // parity crossing list exceeded its capacity
   kErrEmpty = 16u,
   kErrCorruptTree = 32u,      // a node or leaf reference out of range, or a walk that never ends
+  kErrDispatch = 64u,         // a block's tile dispatch waited past its limit
 };
 
 constexpr int kWarp = 32;
@@ -192,55 +193,117 @@ __device__ __forceinline__ bool column_crossing(f3 a, f3 b, f3 c, float px, floa
 }
 
 // ---------------------------------------------------------------------------------------------
-// Triangle record for distance queries: 64 bytes, four float4s, in BVH leaf order.
+// Triangle record of the winding-number hierarchy: 64 bytes, four float4s, in BVH leaf order.
 //   r0 = (v0, 1/|e1|^2)    e1 = v1 - v0
 //   r1 = (e1, 1/|e2|^2)    e2 = v2 - v0
 //   r2 = (e2, 1/|e3|^2)    e3 = v2 - v1
 //   r3 = (n,  1/|n|^2)     n = e1 x e2; 1/|n|^2 = 0 marks a degenerate triangle
-// Squared distance: inside the face's prism it is (ap . n)^2 / |n|^2, otherwise the minimum over
-// the three edges of |ap - clamp(ap . e / |e|^2, 0, 1) e|^2. Branch-free, so every lane of a warp
-// executes the same instructions for the same triangle.
 struct TriRec {
   float4 r0, r1, r2, r3;
 };
 
 __device__ __forceinline__ float inv_or_zero(float x) { return x > 0.0f ? 1.0f / x : 0.0f; }
 
-__device__ __forceinline__ float seg_dist2(float px, float py, float pz, float ex, float ey, float ez, float inv_len2) {
-  float t = (px * ex + py * ey + pz * ez) * inv_len2;
-  t = fminf(fmaxf(t, 0.0f), 1.0f);
-  const float dx = px - t * ex, dy = py - t * ey, dz = pz - t * ez;
-  return dx * dx + dy * dy + dz * dz;
+// ---------------------------------------------------------------------------------------------
+// Triangle record for distance queries: 80 bytes, five float4s, in BVH leaf order. Each triangle
+// is stored in its own orthonormal frame: origin at vertex A, u along the longest edge AB, v in
+// the triangle's plane towards C, h along the unit normal. In that frame the triangle is
+// A = (0, 0), B = (b, 0), C = (c1, c2) with c2 >= 0 and 0 <= c1 <= b.
+//   q0 = (A, b)
+//   q1 = (e_u, c1)
+//   q2 = (e_v, c2)
+//   q3 = (e_h, c1 - b)
+//   q4 = (c1 / |AC|^2, c2 / |AC|^2, (c1 - b) / |BC|^2, c2 / |BC|^2)   (0 for a zero-length edge)
+// A point's squared distance is h^2 plus the squared in-plane distance from (u, v) to the 2D
+// triangle: zero inside it, else the nearest of the three clamped edge projections. A collinear
+// or point-like triangle has c2 = 0 and is never inside (the inside test is strict), so only its
+// edges count, and with c2 = 0 those are pieces of the u axis. The frame is computed in FP64 from
+// the FP32 vertices and then rounded; A is the exact input vertex.
+//
+// The frame makes a query cheap where the traversal spends its time: a lane holds several cells
+// of one (x, y) column, so the x and y parts of u, v and h are formed once per lane and each cell
+// adds its z term with one FMA; the plane bound h^2 used to skip a triangle is the first step of
+// the full test rather than extra work.
+struct DistTri {
+  float4 q0, q1, q2, q3, q4;
+};
+
+// Squared distance from (u, v) to the 2D triangle (0, 0), (b, 0), (c1, c2) of a DistTri (q4 holds
+// the edge projection factors). Branch-free: every lane executes the same instructions.
+__device__ __forceinline__ float inplane_dist2(float u, float v, float b, float c1, float c2, float bc,
+                                               const float4 &k) {
+  const float du = u - fminf(fmaxf(u, 0.0f), b);  // edge AB on the u axis
+  const float d_ab = fmaf(du, du, v * v);
+  const float s1 = __saturatef(fmaf(v, k.y, u * k.x));  // edge AC
+  const float x1 = fmaf(-s1, c1, u), y1 = fmaf(-s1, c2, v);
+  const float d_ac = fmaf(x1, x1, y1 * y1);
+  const float ub = u - b;  // edge BC
+  const float s2 = __saturatef(fmaf(v, k.w, ub * k.z));
+  const float x2 = fmaf(-s2, bc, ub), y2 = fmaf(-s2, c2, v);
+  const float d_bc = fmaf(x2, x2, y2 * y2);
+  const bool inside = (v > 0.0f) & (fmaf(c2, u, -c1 * v) > 0.0f) & (fmaf(bc, v, -c2 * ub) > 0.0f);
+  return inside ? 0.0f : fminf(fminf(d_ab, d_ac), d_bc);
 }
 
-__device__ __forceinline__ float point_tri_dist2(float px, float py, float pz, const float4 &r0, const float4 &r1,
-                                                 const float4 &r2, const float4 &r3) {
-  const float ax = px - r0.x, ay = py - r0.y, az = pz - r0.z;  // ap
-  const float d_ab = seg_dist2(ax, ay, az, r1.x, r1.y, r1.z, r0.w);
-  const float d_ac = seg_dist2(ax, ay, az, r2.x, r2.y, r2.z, r1.w);
-  const float bx = ax - r1.x, by = ay - r1.y, bz = az - r1.z;  // bp
-  const float e3x = r2.x - r1.x, e3y = r2.y - r1.y, e3z = r2.z - r1.z;
-  const float d_bc = seg_dist2(bx, by, bz, e3x, e3y, e3z, r2.w);
-  // Barycentric tests against n: beta' = (ap x e2) . n, gamma' = (e1 x ap) . n
-  const float cx0 = ay * r2.z - az * r2.y, cy0 = az * r2.x - ax * r2.z, cz0 = ax * r2.y - ay * r2.x;
-  const float beta = cx0 * r3.x + cy0 * r3.y + cz0 * r3.z;
-  const float cx1 = r1.y * az - r1.z * ay, cy1 = r1.z * ax - r1.x * az, cz1 = r1.x * ay - r1.y * ax;
-  const float gamma = cx1 * r3.x + cy1 * r3.y + cz1 * r3.z;
-  const float h = ax * r3.x + ay * r3.y + az * r3.z;
-  const bool inside = (r3.w > 0.0f) & (beta >= 0.0f) & (gamma >= 0.0f) & ((beta + gamma) * r3.w <= 1.0f);
-  const float d_face = inside ? h * h * r3.w : __int_as_float(0x7f800000);
-  return fminf(fminf(d_face, d_ab), fminf(d_ac, d_bc));
+// The DistTri of triangle (a, b, c), built in FP64.
+__device__ inline DistTri make_dist_tri(float3 fa, float3 fb, float3 fc) {
+  struct D3 {
+    double x, y, z;
+  };
+  auto sub = [](D3 p, D3 q) { return D3{p.x - q.x, p.y - q.y, p.z - q.z}; };
+  auto dot = [](D3 p, D3 q) { return p.x * q.x + p.y * q.y + p.z * q.z; };
+  auto cross = [](D3 p, D3 q) { return D3{p.y * q.z - p.z * q.y, p.z * q.x - p.x * q.z, p.x * q.y - p.y * q.x}; };
+  auto scale = [](D3 p, double s) { return D3{p.x * s, p.y * s, p.z * s}; };
+  D3 v[3] = {{fa.x, fa.y, fa.z}, {fb.x, fb.y, fb.z}, {fc.x, fc.y, fc.z}};
+  // Rotate the vertices so that AB is the longest edge (C then projects inside [A, B]).
+  const double l0 = dot(sub(v[1], v[0]), sub(v[1], v[0]));  // v0 v1
+  const double l1 = dot(sub(v[2], v[1]), sub(v[2], v[1]));  // v1 v2
+  const double l2 = dot(sub(v[0], v[2]), sub(v[0], v[2]));  // v2 v0
+  const int r = (l0 >= l1 && l0 >= l2) ? 0 : (l1 >= l2 ? 1 : 2);
+  const D3 A = v[r], B = v[(r + 1) % 3], C = v[(r + 2) % 3];
+  const D3 ab = sub(B, A), ac = sub(C, A);
+  const double b = sqrt(dot(ab, ab));
+  D3 eu{1.0, 0.0, 0.0}, ev{0.0, 1.0, 0.0};
+  double c1 = 0.0, c2 = 0.0;
+  if (b > 0.0) {
+    eu = scale(ab, 1.0 / b);
+    c1 = dot(ac, eu);
+    const D3 perp = sub(ac, scale(eu, c1));
+    c2 = sqrt(dot(perp, perp));
+    if (c2 > 1e-12 * b) {
+      ev = scale(perp, 1.0 / c2);
+    } else {
+      // Collinear: any unit vector perpendicular to e_u (from the axis e_u is least aligned with).
+      c2 = 0.0;
+      const double ax = fabs(eu.x), ay = fabs(eu.y), az = fabs(eu.z);
+      const D3 axis = (ax <= ay && ax <= az) ? D3{1.0, 0.0, 0.0} : (ay <= az ? D3{0.0, 1.0, 0.0} : D3{0.0, 0.0, 1.0});
+      const D3 w = sub(axis, scale(eu, dot(axis, eu)));
+      ev = scale(w, 1.0 / sqrt(dot(w, w)));
+    }
+  }
+  const D3 eh = cross(eu, ev);
+  const double bc = c1 - b;
+  const double ac2 = c1 * c1 + c2 * c2, bc2 = bc * bc + c2 * c2;
+  const float3 fA = r == 0 ? fa : (r == 1 ? fb : fc);
+  DistTri t;
+  t.q0 = make_float4(fA.x, fA.y, fA.z, float(b));
+  t.q1 = make_float4(float(eu.x), float(eu.y), float(eu.z), float(c1));
+  t.q2 = make_float4(float(ev.x), float(ev.y), float(ev.z), float(c2));
+  t.q3 = make_float4(float(eh.x), float(eh.y), float(eh.z), float(bc));
+  t.q4 = make_float4(ac2 > 0.0 ? float(c1 / ac2) : 0.0f, ac2 > 0.0 ? float(c2 / ac2) : 0.0f,
+                     bc2 > 0.0 ? float(bc / bc2) : 0.0f, bc2 > 0.0 ? float(c2 / bc2) : 0.0f);
+  return t;
 }
 
-// FP32 arithmetic of the routines above, counted as flops (add / sub / mul = 1, FMA = 2; min,
-// max and compares are not counted), for the roofline figure:
-// point_tri_dist2 = 3 (ap) + 3 x 17 (edge: dot 5, scale 1, p - t e 6, |.|^2 5) + 6 (bp, e3)
-//                 + 2 x 14 (cross 9 + dot 5) + 5 (h) + 2 (h^2 w) + 2 (inside test) = 97
-// box_dist2       = 3 x 2 (sub) + 5 (|d|^2) = 11
-// plane bound     = 3 (ap) + 5 (ap . n) + 2 (h^2 w) = 10
-constexpr int kFlopsPointTri = 97;
+// FP32 arithmetic of the distance tests, counted as flops (add / sub / mul = 1, FMA = 2; min, max,
+// saturate and compares are not counted), for the roofline figure. Per cell and triangle:
+// plane bound = 3 (ap) + 5 (h = ap . e_h) + 1 (h^2)                                          =  9
+// full test   = 2 x 5 (u, v) + 4 (edge AB) + 10 (edge AC) + 11 (edge BC) + 6 (inside) + 1     = 42
+//               (on top of the plane bound, whose ap, h and h^2 it reuses)
+// box_dist2   = 3 x 2 (sub) + 5 (|d|^2)                                                      = 11
+constexpr int kFlopsPointTri = 42;
 constexpr int kFlopsPointBox = 11;
-constexpr int kFlopsPointPlane = 10;
+constexpr int kFlopsPointPlane = 9;
 
 // ---------------------------------------------------------------------------------------------
 // BVH node (64 bytes): the boxes of both children plus their references, so one 64-byte read

@@ -6,7 +6,7 @@
 // The warp walks the BVH together: at each node every lane measures its cells against both child
 // boxes, __any_sync decides whether any cell still needs a child, and the child with the smaller
 // warp-minimum box distance (__reduce_min_sync) goes first. Leaves are tested right away by
-// all lanes on the same triangle record (a broadcast 64-byte load), so lanes never diverge. The
+// all lanes on the same triangle record (a broadcast 80-byte load), so lanes never diverge. The
 // deferred child is pushed as (node, child) and its box is re-tested against the tightened
 // bounds when popped. The stack lives in registers, one entry per lane, read with __shfl_sync.
 //
@@ -35,11 +35,18 @@
 namespace sdfb {
 namespace {
 
-// Pass A runs warps independently, so small blocks let the register file hold as many warps as it
-// can (the 4x4x8 and 8x4x4 tiles need about 104 registers: 18 warps per SM in blocks of 2 warps,
-// 16 in blocks of 8). Pass B's block shares one tile: 8 warps.
-constexpr int kThreadsA = 64;
+// Pass A: a block takes chunks of consecutive tiles (a brick of neighbouring tiles) and its warps
+// take tiles from the block's chunk, so the warps sharing an SM's L1 walk overlapping parts of the
+// tree. 10 warps fill the register file twice over at the ~92 registers of the 4-cells-per-lane
+// tiles (20 warps per SM). Pass B's block shares one tile: 8 warps.
+constexpr int kThreadsA = 320;
 constexpr int kWarpsPerBlockA = kThreadsA / kWarp;
+// Tile order within a mesh: bricks of kBrickX x kBrickY x kBrickZ tiles, x fastest inside a brick
+// and across bricks. Tiles of a partial brick beyond the grid have no active cell.
+constexpr int kBrickX = 4, kBrickY = 4, kBrickZ = 2, kBrickTiles = kBrickX * kBrickY * kBrickZ;
+constexpr int kChunkMax = 32;  // tiles per chunk when there are plenty
+constexpr unsigned long long kNoTile = ~0ull;
+constexpr int kDispatchSpin = 1 << 22;  // bound on a warp's wait for its block's next chunk
 constexpr int kThreads = 256;
 constexpr int kSplitBits = 5;  // pass B: 32 subtrees per deferred tile
 constexpr float kInf = __builtin_huge_valf();
@@ -74,10 +81,13 @@ struct TileCells {
     g = M->g;
     const unsigned long long local = tile - B.tile_starts[mesh];
     const int tiles_x = (g.nx + TX - 1) / TX, tiles_y = (g.ny + TY - 1) / TY;
-    const int tx = static_cast<int>(local % tiles_x);
-    const unsigned long long rest = local / tiles_x;
-    const int ty = static_cast<int>(rest % tiles_y);
-    const int tz = static_cast<int>(rest / tiles_y);
+    const int bricks_x = (tiles_x + kBrickX - 1) / kBrickX, bricks_y = (tiles_y + kBrickY - 1) / kBrickY;
+    const unsigned long long brick = local / kBrickTiles;
+    const int w = static_cast<int>(local % kBrickTiles);
+    const unsigned long long rest = brick / bricks_x;
+    const int tx = static_cast<int>(brick % bricks_x) * kBrickX + w % kBrickX;
+    const int ty = static_cast<int>(rest % bricks_y) * kBrickY + (w / kBrickX) % kBrickY;
+    const int tz = static_cast<int>(rest / bricks_y) * kBrickZ + w / (kBrickX * kBrickY);
     vx = tx * TX + lane % TX;
     vy = ty * TY + (lane / TX) % TY;
     vz0 = tz * TZ + lane / kLayer;
@@ -97,7 +107,7 @@ struct TileCells {
 };
 
 template <int VPL, bool COUNT>
-__device__ __forceinline__ void test_leaf(const TriRec *__restrict__ tris, int num_tris, int first, int count,
+__device__ __forceinline__ void test_leaf(const DistTri *__restrict__ tris, int num_tris, int first, int count,
                                           float px, float py, const float (&pz)[VPL], float (&best)[VPL],
                                           WalkStats &ws) {
   if (first < 0 || count > num_tris - first) {
@@ -105,21 +115,31 @@ __device__ __forceinline__ void test_leaf(const TriRec *__restrict__ tris, int n
     return;
   }
   for (int k = 0; k < count; ++k) {
-    const TriRec *tr = tris + first + k;
-    const float4 r0 = __ldg(&tr->r0), r3 = __ldg(&tr->r3);
-    // The squared distance to the triangle's plane, (ap . n)^2 / |n|^2, bounds the squared
-    // distance to the triangle from below: skip the triangle when no cell could improve.
+    const DistTri *tr = tris + first + k;
+    const float4 q0 = __ldg(&tr->q0), q3 = __ldg(&tr->q3), q1 = __ldg(&tr->q1), q2 = __ldg(&tr->q2),
+                 q4 = __ldg(&tr->q4);
+    // The x and y parts of the frame coordinates are shared by the lane's cells.
+    const float ax = px - q0.x, ay = py - q0.y;
+    const float sh = fmaf(ay, q3.y, ax * q3.x);
+    // The squared distance to the triangle's plane, h^2, bounds the squared distance to the
+    // triangle from below: skip the triangle when no cell could improve.
+    float az[VPL], h2[VPL];
     bool need = false;
 #pragma unroll
     for (int v = 0; v < VPL; ++v) {
-      const float h = (px - r0.x) * r3.x + (py - r0.y) * r3.y + (pz[v] - r0.z) * r3.z;
-      need |= h * h * r3.w < best[v];
+      az[v] = pz[v] - q0.z;
+      const float h = fmaf(az[v], q3.z, sh);
+      h2[v] = h * h;
+      need |= h2[v] < best[v];
     }
     if (COUNT) ws.plane_tests += kWarp * VPL;
     if (!__any_sync(kFull, need)) continue;
-    const float4 r1 = __ldg(&tr->r1), r2 = __ldg(&tr->r2);
+    const float su = fmaf(ay, q1.y, ax * q1.x), sv = fmaf(ay, q2.y, ax * q2.x);
 #pragma unroll
-    for (int v = 0; v < VPL; ++v) best[v] = fminf(best[v], point_tri_dist2(px, py, pz[v], r0, r1, r2, r3));
+    for (int v = 0; v < VPL; ++v) {
+      const float u = fmaf(az[v], q1.z, su), w = fmaf(az[v], q2.z, sv);
+      best[v] = fminf(best[v], h2[v] + inplane_dist2(u, w, q0.w, q1.w, q2.w, q3.w, q4));
+    }
     if (COUNT) ws.tri_tests += kWarp * VPL;
   }
 }
@@ -138,7 +158,7 @@ struct TailCheck {
 // early by the tail check with work left (best[] then holds upper bounds); a walk past the limit a
 // correct tree allows stops with the corrupt flag.
 template <int VPL, int STACK, bool COUNT>
-__device__ __forceinline__ bool walk(const Node *__restrict__ nodes, const TriRec *__restrict__ tris, int num_nodes,
+__device__ __forceinline__ bool walk(const Node *__restrict__ nodes, const DistTri *__restrict__ tris, int num_nodes,
                                      int num_tris, int start, TailCheck tail, int lane, float px, float py,
                                      const float (&pz)[VPL], const bool (&active)[VPL], float (&best)[VPL],
                                      WalkStats &ws) {
@@ -287,8 +307,39 @@ __device__ __forceinline__ void flush_stats(const DistanceArgs &a, const WalkSta
   }
 }
 
-// Pass A: one warp per tile, tiles from a global counter; a tile still walking in the pass's tail
-// is deferred to pass B.
+// Hands lane 0 of a warp its next tile. *state packs the block's current chunk (high 32 bits)
+// and the next index within it (low 32 bits); chunks come from the global counter. The warp that
+// draws index == per_chunk moves the block to a new chunk; warps drawing past it wait for that
+// (bounded: past the limit the dispatch error is raised and the warp stops). Returns kNoTile when
+// every chunk has been handed out.
+__device__ unsigned long long next_tile(unsigned long long *state, unsigned long long *chunks,
+                                        unsigned long long per_chunk, unsigned long long total_chunks,
+                                        unsigned long long total_tiles, uint32_t *err) {
+  for (;;) {
+    const unsigned long long old = atomicAdd(state, 1ull);
+    const unsigned long long chunk = old >> 32, idx = old & 0xffffffffull;
+    if (chunk >= total_chunks) return kNoTile;
+    if (idx < per_chunk) {
+      const unsigned long long t = chunk * per_chunk + idx;
+      if (t < total_tiles) return t;
+      continue;  // past the end of the last chunk: draw on until the block moves on
+    }
+    if (idx == per_chunk) {
+      atomicExch(state, atomicAdd(chunks, 1ull) << 32);
+      continue;
+    }
+    const volatile unsigned long long *vs = state;
+    int spin = 0;
+    while ((*vs >> 32) == chunk && spin < kDispatchSpin) ++spin;
+    if (spin == kDispatchSpin) {
+      atomic_or_err(err, kErrDispatch);
+      return kNoTile;
+    }
+  }
+}
+
+// Pass A: warps take tiles from their block's chunk, blocks take chunks from a global counter; a
+// tile still walking in the pass's tail (every chunk handed out) is deferred to pass B.
 template <int TX, int TY, int TZ, int STACK, bool COUNT>
 __global__ __launch_bounds__(kThreadsA) void k_distance(DistanceArgs a) {
   using Cells = TileCells<TX, TY, TZ>;
@@ -296,15 +347,19 @@ __global__ __launch_bounds__(kThreadsA) void k_distance(DistanceArgs a) {
   const int lane = threadIdx.x & 31;
   const BatchDev &B = a.batch;
   WalkStats ws;
-  TailCheck tail{a.tile_counter, B.total_tiles,
+  const unsigned long long total_chunks = (B.total_tiles + a.chunk_tiles - 1) / a.chunk_tiles;
+  TailCheck tail{a.tile_counter, total_chunks,
                  (a.defer_list && a.step_budget > 0) ? static_cast<int>(min(a.step_budget, 1ll << 30)) : 0};
   const TailCheck never{nullptr, 0, 0};
+  __shared__ unsigned long long s_state;
+  if (threadIdx.x == 0) s_state = atomicAdd(a.tile_counter, 1ull) << 32;
+  __syncthreads();
 
   for (;;) {
     unsigned long long tile = 0;
-    if (lane == 0) tile = atomicAdd(a.tile_counter, 1ull);
+    if (lane == 0) tile = next_tile(&s_state, a.tile_counter, a.chunk_tiles, total_chunks, B.total_tiles, a.err);
     tile = __shfl_sync(kFull, tile, 0);
-    if (tile >= B.total_tiles) break;
+    if (tile == kNoTile) break;
     Cells c;
     c.locate(B, tile, lane);
     const MeshRec &M = *c.M;
@@ -452,10 +507,19 @@ cudaError_t launch_shape(const DistanceArgs &a, int num_sms, cudaStream_t st) {
   unsigned long long blocks = static_cast<unsigned long long>(num_sms) * per_sm;
   blocks = std::min<unsigned long long>(blocks, (warps_needed + kWarpsPerBlockA - 1) / kWarpsPerBlockA);
   if (blocks < 1) blocks = 1;
+  // kChunkMax tiles per chunk when there are plenty, fewer when the tiles would not reach every
+  // warp several times over. Pass A uses no shared memory to speak of: all of it goes to L1.
+  static const bool carveout = cudaFuncSetAttribute(k_distance<s.tx, s.ty, s.tz, STACK, COUNT>,
+                                                    cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                    cudaSharedmemCarveoutMaxL1) == cudaSuccess;
+  (void)carveout;
+  DistanceArgs ca = a;
+  ca.chunk_tiles = std::max<unsigned long long>(
+      1, std::min<unsigned long long>(kChunkMax, a.batch.total_tiles / (blocks * kWarpsPerBlockA * 4)));
   cudaError_t e = cudaMemsetAsync(a.tile_counter, 0, sizeof(unsigned long long), st);
   if (e == cudaSuccess && a.defer_list) e = cudaMemsetAsync(a.defer_counters, 0, 2 * sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
-  k_distance<s.tx, s.ty, s.tz, STACK, COUNT><<<static_cast<unsigned>(blocks), kThreadsA, 0, st>>>(a);
+  k_distance<s.tx, s.ty, s.tz, STACK, COUNT><<<static_cast<unsigned>(blocks), kThreadsA, 0, st>>>(ca);
   note_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess || !a.defer_list || a.step_budget <= 0) return e;
@@ -494,7 +558,9 @@ void tile_shape(int id, int &tx, int &ty, int &tz) {
 uint64_t tiles_for(const GridDev &g, int id) {
   int tx, ty, tz;
   tile_shape(id, tx, ty, tz);
-  return uint64_t((g.nx + tx - 1) / tx) * uint64_t((g.ny + ty - 1) / ty) * uint64_t((g.nz + tz - 1) / tz);
+  const uint64_t bx = ((g.nx + tx - 1) / tx + kBrickX - 1) / kBrickX, by = ((g.ny + ty - 1) / ty + kBrickY - 1) / kBrickY,
+                 bz = ((g.nz + tz - 1) / tz + kBrickZ - 1) / kBrickZ;
+  return bx * by * bz * kBrickTiles;
 }
 
 uint64_t defer_capacity_for(uint64_t total_tiles) {

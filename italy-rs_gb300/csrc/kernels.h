@@ -13,6 +13,7 @@
 namespace sdfb {
 
 struct TriRec;
+struct DistTri;
 struct Node;
 
 // Count of kernel launches issued by this library (every launcher calls note_launch once per
@@ -69,7 +70,7 @@ struct MeshRec {
   int bvh_nodes;          // node count of the hierarchy holding this mesh (root < bvh_nodes)
   // The hierarchy holding this mesh: the batch's combined tree, or the mesh's resident tree.
   const Node *nodes;
-  const TriRec *tris;
+  const DistTri *tris;
   int bvh_tris;           // records in that hierarchy
   // GWN: the hierarchy holding this mesh's caps
   int cap_nodes_n, cap_inner_n, cap_recs_n;
@@ -107,18 +108,21 @@ __host__ __device__ __forceinline__ int find_mesh(const uint64_t *starts, int n,
 // one binary radix tree; each mesh's subtree is entered through its virtual root node, stored
 // after the inner nodes.
 struct BvhDev {
-  TriRec *tris = nullptr;          // T_total records in leaf order
+  DistTri *dtris = nullptr;        // distance hierarchy: T_total records in leaf order
+  TriRec *tris = nullptr;          // winding-number hierarchy: T_total records in leaf order
   Node *nodes = nullptr;           // (T_total - 1) inner nodes + M virtual roots
   uint32_t *leaf_order = nullptr;  // local (per-mesh) triangle index of each record
   uint32_t *bounds = nullptr;      // 6 ordered-uint words per mesh: centroid min xyz, max xyz
-  float *node_area = nullptr;      // optional: total triangle area per inner node
+  float *node_area = nullptr;      // winding-number hierarchy: total triangle area per inner node
   int num_inner = 0;               // max(T_total - 1, 0)
   int num_nodes = 0;               // num_inner + M
 };
 
 size_t lbvh_temp_bytes(uint64_t total_tris, int num_meshes);
-size_t lbvh_bytes(uint64_t total_tris, int num_meshes, bool with_areas);
-void lbvh_bind(BvhDev &b, void *mem, uint64_t total_tris, int num_meshes, bool with_areas);
+// winding = false: the distance hierarchy (DistTri records); true: the winding-number hierarchy
+// (TriRec records and per-node triangle areas).
+size_t lbvh_bytes(uint64_t total_tris, int num_meshes, bool winding);
+void lbvh_bind(BvhDev &b, void *mem, uint64_t total_tris, int num_meshes, bool winding);
 cudaError_t lbvh_build(const BatchDev &batch, BvhDev &b, void *temp, size_t temp_bytes, uint32_t *err,
                        cudaStream_t st);
 
@@ -143,7 +147,8 @@ struct DistanceArgs {
   const uint64_t *col_start;  // parity
   const float *col_z;
   uint32_t *err;
-  unsigned long long *tile_counter;   // zeroed by the launcher
+  unsigned long long *tile_counter;   // pass A's chunk counter, zeroed by the launcher
+  unsigned long long chunk_tiles;     // tiles per chunk (set by the launcher)
   unsigned long long *work_counters;  // optional: [0] box, [1] triangle, [3] plane tests (lanes)
   // Deferral of long tiles (none when defer_list is null or step_budget <= 0): every step_budget
   // traversal steps a walk checks whether all tiles have been handed out and, if so, defers its

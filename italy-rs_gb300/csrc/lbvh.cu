@@ -2,7 +2,8 @@
 // of src/convert/sdf_baker.cpp:170-193, which builds one acceleration structure per call).
 //
 //   1. k_prep      gathers each indexed triangle of each mesh, checks indices and finiteness,
-//                  writes its 64-byte distance record and box, and reduces per-mesh centroid bounds.
+//                  writes its box (and, for the winding-number hierarchy, its 64-byte record), and
+//                  reduces per-mesh centroid bounds.
 //   2. k_morton    key = (mesh << 30) | 30-bit Morton code of the box centre in its mesh's bounds.
 //   3. radix sort  (key, triangle) pairs, stable: meshes end up contiguous, each in Morton order.
 //   4. k_hierarchy binary radix tree over all keys (Karras 2012, "Maximizing Parallelism in the
@@ -14,7 +15,8 @@
 //   7. k_roots     one virtual root node per mesh, after the inner nodes, whose first child is
 //                  the mesh's subtree (or leaf) and whose second child is empty; traversal of a
 //                  mesh starts there.
-//   8. k_gather    triangle records in leaf order.
+//   8. k_gather    triangle records in leaf order: 80-byte frame records (DistTri) for the
+//                  distance hierarchy, the k_prep records for the winding-number hierarchy.
 //   9. k_areas     (optional) total triangle area per inner node.
 #include <algorithm>
 #include <cstdint>
@@ -110,19 +112,21 @@ __global__ __launch_bounds__(kThreads) void k_prep(BatchDev B, TriRec *__restric
     const bool finite = isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(b.x) && isfinite(b.y) &&
                         isfinite(b.z) && isfinite(c.x) && isfinite(c.y) && isfinite(c.z);
     if (!finite) atomic_or_err(err, kErrNonFinite);
-    const float e1x = b.x - a.x, e1y = b.y - a.y, e1z = b.z - a.z;
-    const float e2x = c.x - a.x, e2y = c.y - a.y, e2z = c.z - a.z;
-    const float e3x = c.x - b.x, e3y = c.y - b.y, e3z = c.z - b.z;
-    const float nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
-    TriRec r;
-    r.r0 = make_float4(a.x, a.y, a.z, inv_or_zero(e1x * e1x + e1y * e1y + e1z * e1z));
-    r.r1 = make_float4(e1x, e1y, e1z, inv_or_zero(e2x * e2x + e2y * e2y + e2z * e2z));
-    r.r2 = make_float4(e2x, e2y, e2z, inv_or_zero(e3x * e3x + e3y * e3y + e3z * e3z));
-    const float n2 = nx * nx + ny * ny + nz * nz;
-    // A face region is only used when the normal is well above rounding noise.
-    const float scale = fmaxf(e1x * e1x + e1y * e1y + e1z * e1z, e2x * e2x + e2y * e2y + e2z * e2z);
-    r.r3 = make_float4(nx, ny, nz, (n2 > 1e-12f * scale * scale) ? 1.0f / n2 : 0.0f);
-    rec[t] = r;
+    if (rec) {
+      const float e1x = b.x - a.x, e1y = b.y - a.y, e1z = b.z - a.z;
+      const float e2x = c.x - a.x, e2y = c.y - a.y, e2z = c.z - a.z;
+      const float e3x = c.x - b.x, e3y = c.y - b.y, e3z = c.z - b.z;
+      const float nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+      TriRec r;
+      r.r0 = make_float4(a.x, a.y, a.z, inv_or_zero(e1x * e1x + e1y * e1y + e1z * e1z));
+      r.r1 = make_float4(e1x, e1y, e1z, inv_or_zero(e2x * e2x + e2y * e2y + e2z * e2z));
+      r.r2 = make_float4(e2x, e2y, e2z, inv_or_zero(e3x * e3x + e3y * e3y + e3z * e3z));
+      const float n2 = nx * nx + ny * ny + nz * nz;
+      // The normal counts only when it is well above rounding noise.
+      const float scale = fmaxf(e1x * e1x + e1y * e1y + e1z * e1z, e2x * e2x + e2y * e2y + e2z * e2z);
+      r.r3 = make_float4(nx, ny, nz, (n2 > 1e-12f * scale * scale) ? 1.0f / n2 : 0.0f);
+      rec[t] = r;
+    }
     const float4 l = make_float4(fminf(fminf(a.x, b.x), c.x), fminf(fminf(a.y, b.y), c.y),
                                  fminf(fminf(a.z, b.z), c.z), 0.0f);
     const float4 h = make_float4(fmaxf(fmaxf(a.x, b.x), c.x), fmaxf(fmaxf(a.y, b.y), c.y),
@@ -384,12 +388,24 @@ __global__ void k_roots(BatchDev B, int num_inner, const uint32_t *__restrict__ 
 
 __global__ __launch_bounds__(kThreads) void k_gather(BatchDev B, const uint32_t *__restrict__ vals,
                                                      const TriRec *__restrict__ rec, TriRec *__restrict__ out,
-                                                     uint32_t *__restrict__ order) {
+                                                     DistTri *__restrict__ dout, uint32_t *__restrict__ order) {
   const uint64_t k = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
   if (k >= B.total_tris) return;
   const uint32_t t = vals ? vals[k] : static_cast<uint32_t>(k);
-  out[k] = rec[t];
-  order[k] = static_cast<uint32_t>(t - B.tri_starts[find_mesh(B.tri_starts, B.num_meshes, t)]);
+  const int mesh = find_mesh(B.tri_starts, B.num_meshes, t);
+  const uint64_t lt = t - B.tri_starts[mesh];
+  if (out) out[k] = rec[t];
+  if (dout) {
+    // The frame is built from the input vertices (k_prep has flagged bad indices already).
+    const MeshRec &M = B.recs[mesh];
+    const uint32_t V = M.num_verts;
+    uint32_t i0 = __ldg(M.idx + 3 * lt), i1 = __ldg(M.idx + 3 * lt + 1), i2 = __ldg(M.idx + 3 * lt + 2);
+    i0 = i0 < V ? i0 : 0;
+    i1 = i1 < V ? i1 : 0;
+    i2 = i2 < V ? i2 : 0;
+    dout[k] = make_dist_tri(load3(M.verts, i0), load3(M.verts, i1), load3(M.verts, i2));
+  }
+  order[k] = static_cast<uint32_t>(lt);
 }
 
 // Total triangle area of every inner node, bottom-up like k_refit (bounds the solid angle a
@@ -422,24 +438,25 @@ inline unsigned blocks_for(size_t n) { return static_cast<unsigned>((n + kThread
 
 size_t lbvh_temp_bytes(uint64_t total_tris, int num_meshes) { return temp_layout(total_tris, num_meshes, nullptr, nullptr); }
 
-size_t lbvh_bytes(uint64_t T, int M, bool with_areas) {
+size_t lbvh_bytes(uint64_t T, int M, bool winding) {
   const size_t n = std::max<uint64_t>(T, 1), m = std::max<uint64_t>(T, 2) - 1;
-  return align256(n * sizeof(TriRec)) + align256((m + M) * sizeof(Node)) + align256(n * 4) +
-         align256(size_t(M) * 6 * 4) + (with_areas ? align256(m * sizeof(float)) : 0);
+  return align256(n * (winding ? sizeof(TriRec) : sizeof(DistTri))) + align256((m + M) * sizeof(Node)) +
+         align256(n * 4) + align256(size_t(M) * 6 * 4) + (winding ? align256(m * sizeof(float)) : 0);
 }
 
-void lbvh_bind(BvhDev &b, void *mem, uint64_t T, int M, bool with_areas) {
+void lbvh_bind(BvhDev &b, void *mem, uint64_t T, int M, bool winding) {
   const size_t n = std::max<uint64_t>(T, 1), m = std::max<uint64_t>(T, 2) - 1;
   char *p = static_cast<char *>(mem);
-  b.tris = reinterpret_cast<TriRec *>(p);
-  p += align256(n * sizeof(TriRec));
+  b.tris = winding ? reinterpret_cast<TriRec *>(p) : nullptr;
+  b.dtris = winding ? nullptr : reinterpret_cast<DistTri *>(p);
+  p += align256(n * (winding ? sizeof(TriRec) : sizeof(DistTri)));
   b.nodes = reinterpret_cast<Node *>(p);
   p += align256((m + M) * sizeof(Node));
   b.leaf_order = reinterpret_cast<uint32_t *>(p);
   p += align256(n * 4);
   b.bounds = reinterpret_cast<uint32_t *>(p);
   p += align256(size_t(M) * 6 * 4);
-  b.node_area = with_areas ? reinterpret_cast<float *>(p) : nullptr;
+  b.node_area = winding ? reinterpret_cast<float *>(p) : nullptr;
   b.num_inner = T >= 2 ? static_cast<int>(T - 1) : 0;
   b.num_nodes = b.num_inner + M;
 }
@@ -455,7 +472,7 @@ cudaError_t lbvh_build(const BatchDev &B, BvhDev &b, void *temp, size_t temp_byt
   cudaError_t e;
   k_init_bounds<<<(6 * M + 255) / 256, 256, 0, st>>>(b.bounds, M);
   note_launch();
-  k_prep<<<blocks_for(T), kThreads, 0, st>>>(B, t.rec, t.lo, t.hi, b.bounds, err);
+  k_prep<<<blocks_for(T), kThreads, 0, st>>>(B, b.tris ? t.rec : nullptr, t.lo, t.hi, b.bounds, err);
   note_launch();
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   const int n = static_cast<int>(T);
@@ -488,7 +505,7 @@ cudaError_t lbvh_build(const BatchDev &B, BvhDev &b, void *temp, size_t temp_byt
   }
   k_roots<<<(M + 127) / 128, 128, 0, st>>>(B, b.num_inner, vals, t.lo, t.hi, t.ilo, t.ihi, t.subtree, b.nodes, err);
   note_launch();
-  k_gather<<<blocks_for(T), kThreads, 0, st>>>(B, vals, t.rec, b.tris, b.leaf_order);
+  k_gather<<<blocks_for(T), kThreads, 0, st>>>(B, vals, t.rec, b.tris, b.dtris, b.leaf_order);
   note_launch();
   if (b.node_area && T >= 2) {
     if ((e = cudaMemsetAsync(t.visits, 0, sizeof(int) * (T - 1), st)) != cudaSuccess) return e;

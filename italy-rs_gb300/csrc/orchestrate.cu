@@ -207,7 +207,7 @@ void make_layout(sdfb_ctx *ctx, const std::vector<PlanMesh> &ms, const sdfb_opts
     r.cap_root = -1;
     if (p.bvh) {
       r.nodes = p.bvh->nodes;
-      r.tris = p.bvh->tris;
+      r.tris = p.bvh->dtris;
       r.bvh_nodes = p.bvh->num_nodes;
       r.bvh_tris = p.bvh->num_tris;
       r.root = p.bvh->root;
@@ -286,7 +286,7 @@ void bind_built(Layout &L, const BvhDev &bvh, const BvhDev *caps) {
   for (auto &r : L.recs) {
     if (bvh.nodes) {
       r.nodes = bvh.nodes;
-      r.tris = bvh.tris;
+      r.tris = bvh.dtris;
       r.bvh_nodes = bvh.num_nodes;
       r.bvh_tris = static_cast<int>(L.tri.back());
     }
@@ -524,6 +524,7 @@ sdfb_status finish_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, const Ba
   if (h_err & kErrStackOverflow)
     return ctx_fail(ctx, SDFB_ERR_OVERFLOW, "BVH traversal stack overflow (depth > %d)", S.stack);
   if (h_err & kErrCorruptTree) return ctx_fail(ctx, SDFB_ERR_INTERNAL, "BVH walk met an invalid reference");
+  if (h_err & kErrDispatch) return ctx_fail(ctx, SDFB_ERR_INTERNAL, "distance tile dispatch timed out");
   if (stats) {
     sdfb_stats sv;
     std::memset(&sv, 0, sizeof sv);
@@ -592,7 +593,7 @@ sdfb_status run_batch(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &ms,
 // ---------------------------------------------------------------------------------------------
 // Resident hierarchies (serving).
 
-size_t resident_bytes(uint64_t tris, bool with_areas) { return lbvh_bytes(tris, 1, with_areas); }
+size_t resident_bytes(uint64_t tris, bool winding) { return lbvh_bytes(tris, 1, winding); }
 
 sdfb_status build_resident(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, const PlanMesh &p, void *mem,
                            ResidentBvh &out, void *cap_mem, ResidentBvh &cap_out) {
@@ -638,6 +639,7 @@ sdfb_status build_resident(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, const 
     lbvh_bind(b, m, T, 1, areas);
     CK(lbvh_build(B, b, ws.build_tmp.p, ws.build_tmp.cap, static_cast<uint32_t *>(ws.misc.p), st));
     o.nodes = b.nodes;
+    o.dtris = b.dtris;
     o.tris = b.tris;
     o.leaf_order = b.leaf_order;
     o.node_area = b.node_area;
