@@ -605,13 +605,15 @@ def main(argv=None):
     ho = [torch.empty(c, dtype=torch.uint8).pin_memory().numpy().reshape(g.shape) for c, g in zip(cells, grids)]
     for _ in range(2):
         ctx.bake_batch(hmeshes, grids, opts, out=(hd, ho))
-    e2e_s = []
+    e2e_s, e2e_dev_ms = [], []
     for _ in range(max(3, args.steps // 2)):
         flush.fill_(1.0)
         torch.cuda.synchronize()
+        est = new_stats(sdfb)
         t0 = time.perf_counter()
-        ctx.bake_batch(hmeshes, grids, opts, out=(hd, ho))
+        ctx.bake_batch(hmeshes, grids, opts, out=(hd, ho), stats=est)
         e2e_s.append(time.perf_counter() - t0)
+        e2e_dev_ms.append(est.ms_total)
     e2e_value, _ = aggregate(total_cells * len(e2e_s), sum(e2e_s), red_max, red_sum)
     h2d = int(sum(v.nbytes + i.nbytes for v, i in hmeshes))
     stage(f"e2e: {1e3 * statistics.mean(e2e_s):.1f} ms per step")
@@ -696,7 +698,8 @@ def main(argv=None):
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": int(total_cells * 5), "ms_per_step": 1e3 * statistics.mean(e2e_s)},
+                "d2h_bytes_per_step": int(total_cells * 5), "ms_per_step": 1e3 * statistics.mean(e2e_s),
+                "device_ms_per_step": statistics.mean(e2e_dev_ms)},
         "clocks": clk,
         "gpu_launches": int(sum(launches)),
         "graph_replayed_steps": int(sum(replayed)),
