@@ -2,10 +2,10 @@
 // src/render/kernels/sdf_bake.cu:39-51 with the exact Euclidean distance).
 //
 // Work unit: a warp owns a tile of TX x TY x TZ cells (32 lanes, VPL cells per lane stacked in
-// z) taken from a global counter, so long and short tiles balance across the persistent grid.
-// The warp walks the BVH together: at each node every lane measures its cells against both child
-// boxes, __any_sync decides whether any cell still needs a child, and the child with the smaller
-// warp-minimum box distance (__reduce_min_sync) goes first. Leaves are tested right away by
+// z) taken from its block's chunk of neighbouring tiles, so long and short tiles balance across the
+// persistent grid. The warp walks the BVH together: at each node every lane measures its cells
+// against both child boxes, __any_sync decides whether any cell still needs a child, and the child
+// whose box is nearer the tile's centre goes first. Leaves are tested right away by
 // all lanes on the same triangle record (a broadcast 80-byte load), so lanes never diverge. The
 // deferred child is pushed as (node, child) and its box is re-tested against the tightened
 // bounds when popped. The stack lives in registers, one entry per lane, read with __shfl_sync.
@@ -74,6 +74,7 @@ struct TileCells {
   int vx, vy, vz0;  // this lane's column and first z; cell v is at z = vz0 + v * kLanesZ
   float px, py, pz[VPL];
   bool active[VPL];
+  float cx, cy, cz;  // tile centre
 
   __device__ __forceinline__ void locate(const BatchDev &B, unsigned long long tile, int lane) {
     const int mesh = find_mesh(B.tile_starts, B.num_meshes, tile);
@@ -88,6 +89,9 @@ struct TileCells {
     const int tx = static_cast<int>(brick % bricks_x) * kBrickX + w % kBrickX;
     const int ty = static_cast<int>(rest % bricks_y) * kBrickY + (w / kBrickX) % kBrickY;
     const int tz = static_cast<int>(rest / bricks_y) * kBrickZ + w / (kBrickX * kBrickY);
+    cx = g.ox + (float(tx * TX) + 0.5f * TX) * g.voxel;
+    cy = g.oy + (float(ty * TY) + 0.5f * TY) * g.voxel;
+    cz = g.oz + (float(tz * TZ) + 0.5f * TZ) * g.voxel;
     vx = tx * TX + lane % TX;
     vy = ty * TY + (lane / TX) % TY;
     vz0 = tz * TZ + lane / kLayer;
@@ -159,8 +163,8 @@ struct TailCheck {
 // correct tree allows stops with the corrupt flag.
 template <int VPL, int STACK, bool COUNT>
 __device__ __forceinline__ bool walk(const Node *__restrict__ nodes, const DistTri *__restrict__ tris, int num_nodes,
-                                     int num_tris, int start, TailCheck tail, int lane, float px, float py,
-                                     const float (&pz)[VPL], const bool (&active)[VPL], float (&best)[VPL],
+                                     int num_tris, int start, TailCheck tail, int lane, float tcx, float tcy,
+                                     float tcz, float px, float py, const float (&pz)[VPL], float (&best)[VPL],
                                      WalkStats &ws) {
   static_assert(STACK == 32 || STACK == 64, "stack depth is one or two registers per lane");
   // A correct tree expands each inner node at most once per walk and pops at most once per push.
@@ -213,7 +217,6 @@ __device__ __forceinline__ bool walk(const Node *__restrict__ nodes, const DistT
     const float4 n0 = __ldg(&np->n0), n1 = __ldg(&np->n1), n2 = __ldg(&np->n2);
     const int4 n3 = __ldg(&np->n3);
     float d0[VPL], d1[VPL];
-    float m0 = kInf, m1 = kInf;
     bool w0 = false, w1 = false;
 #pragma unroll
     for (int v = 0; v < VPL; ++v) {
@@ -221,16 +224,13 @@ __device__ __forceinline__ bool walk(const Node *__restrict__ nodes, const DistT
       d1[v] = box_dist2(px, py, pz[v], n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
       w0 |= d0[v] < best[v];
       w1 |= d1[v] < best[v];
-      if (active[v]) {
-        m0 = fminf(m0, d0[v]);
-        m1 = fminf(m1, d1[v]);
-      }
     }
     if (COUNT) ws.box_tests += 2 * kWarp * VPL;
     w0 = __any_sync(kFull, w0) && n3.z >= 0;
     w1 = __any_sync(kFull, w1) && n3.w >= 0;
-    const bool second_first =
-        __reduce_min_sync(kFull, __float_as_uint(m1)) < __reduce_min_sync(kFull, __float_as_uint(m0));
+    // Near child first: the one whose box is nearer the tile's centre (the same on every lane).
+    const bool second_first = box_dist2(tcx, tcy, tcz, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w) <
+                              box_dist2(tcx, tcy, tcz, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
     const int near_ref = second_first ? n3.y : n3.x, near_cnt = second_first ? n3.w : n3.z;
     const int far_ref = second_first ? n3.x : n3.y, far_cnt = second_first ? n3.z : n3.w;
     bool near_w = second_first ? w1 : w0, far_w = second_first ? w0 : w1;
@@ -366,8 +366,8 @@ __global__ __launch_bounds__(kThreadsA) void k_distance(DistanceArgs a) {
     float best[VPL];
 #pragma unroll
     for (int v = 0; v < VPL; ++v) best[v] = c.active[v] ? kInf : -1.0f;
-    bool done = walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, M.root, tail, lane, c.px, c.py,
-                                        c.pz, c.active, best, ws);
+    bool done = walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, M.root, tail, lane, c.cx, c.cy,
+                                        c.cz, c.px, c.py, c.pz, best, ws);
     if (!done) {
       unsigned long long slot = 0;
       if (lane == 0) slot = atomicAdd(a.defer_counters, 1ull);
@@ -380,8 +380,8 @@ __global__ __launch_bounds__(kThreadsA) void k_distance(DistanceArgs a) {
         continue;
       }
       // The list is full: finish the tile here, from the bounds found so far.
-      walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, M.root, never, lane, c.px, c.py, c.pz,
-                              c.active, best, ws);
+      walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, M.root, never, lane, c.cx, c.cy, c.cz, c.px,
+                              c.py, c.pz, best, ws);
     }
     store_cells<TX, TY, TZ>(a, c, best);
   }
@@ -474,8 +474,8 @@ __global__ __launch_bounds__(kThreads) void k_distance_deferred(DistanceArgs a) 
         cur = ref;
       }
       if (walk_it)
-        walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, cur, TailCheck{nullptr, 0, 0}, lane, c.px,
-                                c.py, c.pz, c.active, best, ws);
+        walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, cur, TailCheck{nullptr, 0, 0}, lane, c.cx,
+                                c.cy, c.cz, c.px, c.py, c.pz, best, ws);
 #pragma unroll
       for (int v = 0; v < VPL; ++v)
         if (c.active[v]) atomicMin(&s_best[v * kWarp + lane], __float_as_uint(best[v]));
@@ -558,8 +558,9 @@ void tile_shape(int id, int &tx, int &ty, int &tz) {
 uint64_t tiles_for(const GridDev &g, int id) {
   int tx, ty, tz;
   tile_shape(id, tx, ty, tz);
-  const uint64_t bx = ((g.nx + tx - 1) / tx + kBrickX - 1) / kBrickX, by = ((g.ny + ty - 1) / ty + kBrickY - 1) / kBrickY,
-                 bz = ((g.nz + tz - 1) / tz + kBrickZ - 1) / kBrickZ;
+  const uint64_t bx = ((g.nx + tx - 1) / tx + kBrickX - 1) / kBrickX;
+  const uint64_t by = ((g.ny + ty - 1) / ty + kBrickY - 1) / kBrickY;
+  const uint64_t bz = ((g.nz + tz - 1) / tz + kBrickZ - 1) / kBrickZ;
   return bx * by * bz * kBrickTiles;
 }
 

@@ -198,6 +198,44 @@ def test_degenerate_triangles(ctx, oracle):
     assert np.array_equal(occ.reshape(-1), oracle.occupancy(v, i, (-0.2,) * 3, np.float32(0.05), n))
 
 
+def test_hard_triangles(ctx, oracle):
+    """Slivers, needles, nearly collinear and mixed-scale triangles (each distance record holds
+    its triangle in a frame along the longest edge), then the same soup and grid moved to 1000 on
+    every axis, where FP32 coordinates keep only about 4 decimals: unsigned distances against the
+    FP64 oracle on the same FP32 inputs."""
+    import sdfb
+    rng = np.random.default_rng(11)
+    tris = []
+    for k in range(250):
+        a = rng.uniform(-0.4, 0.4, 3)
+        b = a + rng.normal(0.0, 0.15, 3)
+        kind = k % 5
+        if kind == 0:  # sliver: C within 1e-7 .. 1e-3 of the segment AB
+            c = a + 0.5 * (b - a) + rng.normal(0.0, 1.0, 3) * 10.0 ** rng.uniform(-7, -3)
+        elif kind == 1:  # needle: C next to B
+            c = b + rng.normal(0.0, 1.0, 3) * 1e-6
+        elif kind == 2:  # collinear up to rounding, C anywhere on the line
+            c = a + rng.uniform(-1.0, 2.0) * (b - a)
+        elif kind == 3:  # one short edge AB, C far away
+            b = a + (b - a) * 1e-3
+            c = a + rng.normal(0.0, 0.3, 3)
+        else:
+            c = a + rng.normal(0.0, 0.15, 3)
+        tris.append([a, b, c])
+    v = np.asarray(tris, np.float64).reshape(-1, 3)
+    i = np.arange(len(v), dtype=np.uint32).reshape(-1, 3)
+    n = (24, 24, 24)
+    voxel = np.float32(1.0 / 24)
+    for shift in (0.0, 1000.0):
+        vv = (v + shift).astype(np.float32)
+        origin = (np.float32(-0.5 + shift),) * 3
+        g = sdfb.make_grid(origin, voxel, n)
+        dist, _ = ctx.bake(vv, i, g, sdfb.make_opts(sign_mode=sdfb.SIGN_NONE))
+        d64 = oracle.distance(vv, i, origin, voxel, n)
+        err = np.abs(dist.reshape(-1).astype(np.float64) - d64).max()
+        assert err <= DIST_TOL * diag(voxel, n), (shift, err)
+
+
 def test_error_paths(ctx):
     import sdfb
     v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
