@@ -38,7 +38,8 @@ namespace {
 // Pass A: a block takes chunks of consecutive tiles (a brick of neighbouring tiles) and its warps
 // take tiles from the block's chunk, so the warps sharing an SM's L1 walk overlapping parts of the
 // tree. 10 warps fill the register file twice over at the ~92 registers of the 4-cells-per-lane
-// tiles (20 warps per SM). Pass B's block shares one tile: 8 warps.
+// tiles (20 warps per SM). Pass B's block shares one tile: 16 warps over 64 subtrees, which also
+// keeps a small grid (fewer tiles than the GPU holds warps) busy once its tiles are deferred.
 constexpr int kThreadsA = 320;
 constexpr int kWarpsPerBlockA = kThreadsA / kWarp;
 // Tile order within a mesh: bricks of kBrickX x kBrickY x kBrickZ tiles, x fastest inside a brick
@@ -47,8 +48,8 @@ constexpr int kBrickX = 4, kBrickY = 4, kBrickZ = 2, kBrickTiles = kBrickX * kBr
 constexpr int kChunkMax = 32;  // tiles per chunk when there are plenty
 constexpr unsigned long long kNoTile = ~0ull;
 constexpr int kDispatchSpin = 1 << 22;  // bound on a warp's wait for its block's next chunk
-constexpr int kThreads = 256;
-constexpr int kSplitBits = 5;  // pass B: 32 subtrees per deferred tile
+constexpr int kThreads = 512;
+constexpr int kSplitBits = 6;  // pass B: 64 subtrees per deferred tile
 constexpr float kInf = __builtin_huge_valf();
 
 struct Shape {

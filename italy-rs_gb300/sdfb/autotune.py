@@ -9,7 +9,8 @@ Three parameters of the distance pass trade against each other with the mesh and
   * traversal stack depth (32 or 64 entries): the shallow stack needs fewer registers but a deep
     tree overflows it (the bake then reruns that launch with 64);
   * step budget (traversal steps before a tile is handed to the block-per-tile second pass, or
-    never): a small budget moves more tiles into the pass that splits a tile's walk over a block.
+    never): a small budget moves more tiles into the pass that splits a tile's walk over a block,
+    which pays on small grids (fewer tiles than the GPU holds warps).
 
 For each (log2 triangles, log2 grid edge) bucket of a sweep of displaced spheres and grids, the tuner
 times whole device-buffer bakes (CUDA events on the bake's stream, median of `reps`) under a
@@ -33,15 +34,15 @@ DEFAULT_OUT = os.path.join(os.path.dirname(HERE), "tuning", "gb300.tsv")
 TILES = (1, 2, 3, 4, 5, 6)
 LEAVES = (1, 2, 3, 4, 6, 8)
 STACKS = (32, 64)
-BUDGETS = (-1, 512, 1024, 2048, 4096)
+BUDGETS = (-1, 32, 128, 512, 1024, 2048, 4096)
 START = (4, 3, 64, 1024)  # leaf, tile id (1-based), stack, step budget: the built-in defaults
 
-# (mesh, grid edge): displaced icospheres of levels 3..7 (1,280 .. 327,680 triangles) on 64^3 .. 512^3
+# (mesh, grid edge): displaced icospheres of levels 3..7 (1,280 .. 327,680 triangles) on 32^3 .. 512^3
 # grids, and displaced tori of 131,072 and 1,048,576 triangles (thin tubes; the largest meshes a
 # batch holds) on 128^3 and 256^3 grids
-SWEEP = [(3, 64), (3, 128), (3, 256), (4, 64), (4, 128), (4, 256), (5, 128), (5, 256), (5, 512),
-         (6, 128), (6, 256), (6, 512), (7, 128), (7, 256), (7, 512),
-         ("torus128k", 128), ("torus128k", 256), ("torus1m", 128), ("torus1m", 256)]
+SWEEP = [(3, 32), (3, 64), (3, 128), (3, 256), (4, 64), (4, 128), (4, 256), (5, 32), (5, 64), (5, 128),
+         (5, 256), (5, 512), (6, 32), (6, 64), (6, 128), (6, 256), (6, 512), (7, 32), (7, 64), (7, 128),
+         (7, 256), (7, 512), ("torus128k", 128), ("torus128k", 256), ("torus1m", 128), ("torus1m", 256)]
 QUICK = [(4, 128), (6, 256), (7, 256)]
 TORI = {"torus128k": (512, 128), "torus1m": (1024, 512)}  # nu x nv quads, 2 nu nv triangles
 
