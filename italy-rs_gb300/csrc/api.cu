@@ -203,6 +203,22 @@ sdfb_status upload_caps(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &m
   return SDFB_OK;
 }
 
+// The device address of a page-locked host buffer (cudaHostAlloc, cudaHostRegister, a pinned
+// tensor), or null for pageable memory. The distance kernel writes such a distance output
+// directly: the GPU reaches host memory coherently over NVLink-C2C, so the grid streams to the
+// host while the bake computes instead of in a copy after it. Winding-number meshes keep device
+// outputs, because their band pass reads the distances back; occupancy is always copied (its
+// clear writes single bytes).
+void *mapped_host(void *p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 }  // namespace
 
 sdfb_status device_sign(sdfb_ctx *ctx, const sdfb_opts &o, const float *d_verts, uint32_t V, const uint32_t *d_idx,
@@ -377,16 +393,20 @@ sdfb_status sdfb_bake(sdfb_ctx *ctx, const float *verts, uint32_t num_verts, con
   p.V = num_verts;
   p.T = num_tris;
   p.grid = *grid;
-  p.dist = want_dist ? static_cast<float *>(ctx->out_dist.p) : nullptr;
-  p.occ = want_occ ? static_cast<uint8_t *>(ctx->out_occ.p) : nullptr;
+  float *const direct_dist =
+      (want_dist && p.sign != kSignGwn) ? static_cast<float *>(mapped_host(dist_out)) : nullptr;
+  uint8_t *const direct_occ = nullptr;
+  p.dist = want_dist ? (direct_dist ? direct_dist : static_cast<float *>(ctx->out_dist.p)) : nullptr;
+  p.occ = want_occ ? (direct_occ ? direct_occ : static_cast<uint8_t *>(ctx->out_occ.p)) : nullptr;
   if (p.sign == kSignGwn && want_dist) {
     const sdfb_status s = upload_caps(ctx, st, ms, caps);
     if (s != SDFB_OK) return s;
   }
   const sdfb_status s = run_batch(ctx, st, ms, o, false, stats);
   if (s != SDFB_OK) return s;
-  if (want_dist) CK(cudaMemcpyAsync(dist_out, ctx->out_dist.p, cells * 4, cudaMemcpyDeviceToHost, st));
-  if (want_occ) CK(cudaMemcpyAsync(occ_out, ctx->out_occ.p, cells, cudaMemcpyDeviceToHost, st));
+  if (want_dist && !direct_dist)
+    CK(cudaMemcpyAsync(dist_out, ctx->out_dist.p, cells * 4, cudaMemcpyDeviceToHost, st));
+  if (want_occ && !direct_occ) CK(cudaMemcpyAsync(occ_out, ctx->out_occ.p, cells, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   return SDFB_OK;
 }
@@ -696,7 +716,6 @@ sdfb_status sdfb_bake_batch(sdfb_ctx *ctx, uint32_t count, const sdfb_mesh_desc 
   const sdfb_opts o = opts_or_default(opts);
   const cudaStream_t st = ctx->stream;
   size_t nv = 0, ni = 0;
-  uint64_t nc = 0;
   for (uint32_t m = 0; m < count; ++m) {
     if (!meshes[m].verts || !meshes[m].idx || !grid_ok(&grids[m]))
       return ctx_fail(ctx, SDFB_ERR_INVALID_ARGUMENT, "mesh %u: null pointer or invalid grid", m);
@@ -704,15 +723,14 @@ sdfb_status sdfb_bake_batch(sdfb_ctx *ctx, uint32_t count, const sdfb_mesh_desc 
       return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh %u has no triangles", m);
     nv += size_t(meshes[m].num_verts) * 3;
     ni += size_t(meshes[m].num_tris) * 3;
-    nc += uint64_t(grids[m].nx) * grids[m].ny * grids[m].nz;
   }
   const bool want_dist = dist_outs && !o.no_distance, want_occ = occ_outs && !o.no_occupancy;
   ENSURE(ctx->in_verts, nv * 4);
   ENSURE(ctx->in_idx, ni * 4);
-  if (want_dist) ENSURE(ctx->out_dist, nc * 4);
-  if (want_occ) ENSURE(ctx->out_occ, nc);
   std::vector<PlanMesh> ms(count);
   std::vector<CapBuild> caps(count);
+  std::vector<float *> direct_dist(count, nullptr);
+  std::vector<uint8_t *> direct_occ(count, nullptr);
   bool any_gwn = false;
   size_t ov = 0, oi = 0;
   uint64_t occ_off = 0;
@@ -733,10 +751,9 @@ sdfb_status sdfb_bake_batch(sdfb_ctx *ctx, uint32_t count, const sdfb_mesh_desc 
     p.V = d.num_verts;
     p.T = d.num_tris;
     p.grid = grids[m];
-    const uint64_t cells = uint64_t(p.grid.nx) * p.grid.ny * p.grid.nz;
-    p.dist = (want_dist && dist_outs[m]) ? static_cast<float *>(ctx->out_dist.p) + occ_off : nullptr;
-    p.occ = (want_occ && occ_outs[m]) ? static_cast<uint8_t *>(ctx->out_occ.p) + occ_off : nullptr;
-    if (p.sign == kSignGwn && p.dist) {
+    if (want_dist && dist_outs[m] && p.sign != kSignGwn)
+      direct_dist[m] = static_cast<float *>(mapped_host(dist_outs[m]));
+    if (p.sign == kSignGwn && want_dist && dist_outs[m]) {
       for (size_t k = 0; k < size_t(d.num_tris) * 3; ++k)
         if (d.idx[k] >= d.num_verts) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh %u: triangle index out of range", m);
       build_caps(d.verts, d.num_verts, d.idx, d.num_tris, caps[m]);
@@ -744,7 +761,25 @@ sdfb_status sdfb_bake_batch(sdfb_ctx *ctx, uint32_t count, const sdfb_mesh_desc 
     }
     ov += size_t(d.num_verts) * 3;
     oi += size_t(d.num_tris) * 3;
-    occ_off += cells;
+  }
+  // Outputs: pinned caller buffers directly, the rest through device buffers copied out afterwards.
+  uint64_t staged = 0;
+  for (uint32_t m = 0; m < count; ++m) {
+    const uint64_t cells = uint64_t(grids[m].nx) * grids[m].ny * grids[m].nz;
+    if ((want_dist && dist_outs[m] && !direct_dist[m]) || (want_occ && occ_outs[m] && !direct_occ[m]))
+      staged += cells;
+  }
+  if (staged > 0 && want_dist) ENSURE(ctx->out_dist, staged * 4);
+  if (staged > 0 && want_occ) ENSURE(ctx->out_occ, staged);
+  for (uint32_t m = 0; m < count; ++m) {
+    PlanMesh &p = ms[m];
+    const uint64_t cells = uint64_t(p.grid.nx) * p.grid.ny * p.grid.nz;
+    const bool stage = (want_dist && dist_outs[m] && !direct_dist[m]) || (want_occ && occ_outs[m] && !direct_occ[m]);
+    if (want_dist && dist_outs[m])
+      p.dist = direct_dist[m] ? direct_dist[m] : static_cast<float *>(ctx->out_dist.p) + occ_off;
+    if (want_occ && occ_outs[m])
+      p.occ = direct_occ[m] ? direct_occ[m] : static_cast<uint8_t *>(ctx->out_occ.p) + occ_off;
+    if (stage) occ_off += cells;
   }
   if (any_gwn) {
     const sdfb_status s = upload_caps(ctx, st, ms, caps);
@@ -754,8 +789,9 @@ sdfb_status sdfb_bake_batch(sdfb_ctx *ctx, uint32_t count, const sdfb_mesh_desc 
   if (s != SDFB_OK) return s;
   for (uint32_t m = 0; m < count; ++m) {
     const uint64_t cells = uint64_t(ms[m].grid.nx) * ms[m].grid.ny * ms[m].grid.nz;
-    if (ms[m].dist) CK(cudaMemcpyAsync(dist_outs[m], ms[m].dist, cells * 4, cudaMemcpyDeviceToHost, st));
-    if (ms[m].occ) CK(cudaMemcpyAsync(occ_outs[m], ms[m].occ, cells, cudaMemcpyDeviceToHost, st));
+    if (ms[m].dist && !direct_dist[m])
+      CK(cudaMemcpyAsync(dist_outs[m], ms[m].dist, cells * 4, cudaMemcpyDeviceToHost, st));
+    if (ms[m].occ && !direct_occ[m]) CK(cudaMemcpyAsync(occ_outs[m], ms[m].occ, cells, cudaMemcpyDeviceToHost, st));
   }
   CK(cudaStreamSynchronize(st));
   return SDFB_OK;

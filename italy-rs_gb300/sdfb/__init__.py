@@ -298,12 +298,17 @@ class Context:
             raise SdfbError(st, self.error())
 
     def bake(self, verts, idx, grid: GridDesc, opts: Opts | None = None, want_dist=True, want_occ=True,
-             stats: Stats | None = None):
-        """Host-buffer bake. Returns (dist float32[nz, ny, nx] or None, occ uint8[nz, ny, nx] or None)."""
+             stats: Stats | None = None, out=None):
+        """Host-buffer bake. Returns (dist float32[nz, ny, nx] or None, occ uint8[nz, ny, nx] or None);
+        `out` may pass preallocated (dist, occ) arrays (a pinned distance array is written in place
+        by the bake's kernels)."""
         v = _f32(verts).reshape(-1, 3)
         i = _u32a(idx).reshape(-1, 3)
-        dist = np.empty(grid.shape, np.float32) if want_dist else None
-        occ = np.empty(grid.shape, np.uint8) if want_occ else None
+        if out is not None:
+            dist, occ = out
+        else:
+            dist = np.empty(grid.shape, np.float32) if want_dist else None
+            occ = np.empty(grid.shape, np.uint8) if want_occ else None
         st = self.lib.sdfb_bake(self.h, _ptr(v), len(v), _ptr(i), len(i), C.byref(grid),
                                 C.byref(opts) if opts is not None else None, _ptr(dist), _ptr(occ),
                                 C.byref(stats) if stats is not None else None)
