@@ -236,21 +236,9 @@ __device__ __forceinline__ bool walk(const Node *__restrict__ nodes, const DistT
     const int far_ref = second_first ? n3.x : n3.y, far_cnt = second_first ? n3.z : n3.w;
     bool near_w = second_first ? w1 : w0, far_w = second_first ? w0 : w1;
     cur = -1;
-    if (near_w) {
-      if (near_cnt > 0) {
-        test_leaf<VPL, COUNT>(tris, num_tris, near_ref, near_cnt, px, py, pz, best, ws);
-        if (far_w) {
-          bool w = false;
-#pragma unroll
-          for (int v = 0; v < VPL; ++v) w |= (second_first ? d0[v] : d1[v]) < best[v];
-          far_w = __any_sync(kFull, w);
-        }
-      } else {
-        cur = near_ref;
-      }
-    }
-    if (far_w) {
-      if (cur >= 0) {
+    if (near_w && near_cnt == 0) {
+      cur = near_ref;
+      if (far_w) {
         if (sp < STACK) {
           const int e = (node << 1) | (second_first ? 0 : 1);
           if (STACK == 32 || sp < 32) {
@@ -262,11 +250,21 @@ __device__ __forceinline__ bool walk(const Node *__restrict__ nodes, const DistT
         } else {
           ws.overflow = true;
         }
-      } else if (far_cnt > 0) {
-        test_leaf<VPL, COUNT>(tris, num_tris, far_ref, far_cnt, px, py, pz, best, ws);
-      } else {
-        cur = far_ref;
       }
+      continue;
+    }
+    if (near_w) {
+      test_leaf<VPL, COUNT>(tris, num_tris, near_ref, near_cnt, px, py, pz, best, ws);
+      if (far_w) {
+        bool w = false;
+#pragma unroll
+        for (int v = 0; v < VPL; ++v) w |= (second_first ? d0[v] : d1[v]) < best[v];
+        far_w = __any_sync(kFull, w);
+      }
+    }
+    if (far_w) {
+      if (far_cnt > 0) test_leaf<VPL, COUNT>(tris, num_tris, far_ref, far_cnt, px, py, pz, best, ws);
+      else cur = far_ref;
     }
   }
 }
