@@ -1,12 +1,22 @@
-"""Serving loop: continuous batching over resident meshes. Every served result must equal the
-same bake run alone through the plain entry point (bit for bit: each cell is computed the same
-way whatever else shares the wave)."""
+"""Serving loop: continuous batching over resident meshes. A served result is bit-identical
+whatever else shares its wave (each cell is computed the same way on the mesh's resident
+hierarchy), and equals the same bake run alone through the plain entry point up to rounding: the
+resident hierarchy is built with the leaf size tuned for a 256^3 grid, the plain bake tunes for its
+own grid, and where two triangles nearly tie with an FP32 box bound the walks may keep either."""
 from __future__ import annotations
 
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+
+def assert_same_bake(d, o, d1, o1):
+    """Occupancy and signs identical; distances equal up to the last bits (the bound the
+    leaf-size and tile-shape test uses)."""
+    assert np.array_equal(o, o1)
+    assert np.array_equal(np.signbit(d), np.signbit(d1))
+    assert np.abs(d - d1).max() <= 4e-7
 
 
 def test_served_equals_plain_in_the_mix(ctx):
@@ -18,6 +28,14 @@ def test_served_equals_plain_in_the_mix(ctx):
     with sdfb.Server(ctx, max_inflight=6, wave_voxels_log2=17) as srv:
         ids = [srv.register(v, f) for v, f in meshes]
         assert srv.register(*meshes[1]) == ids[1]  # identical contents: the resident copy
+        alone = []
+        for k in range(3):  # each mesh alone in its wave first
+            n = sizes[k]
+            g = sdfb.make_grid((-0.5,) * 3, 1.0 / n, (n, n + 1, n - 1))
+            d = np.empty(g.shape, np.float32)
+            o = np.empty(g.shape, np.uint8)
+            assert srv.poll(srv.submit(ids[k], g, d, o), 60000)[0]
+            alone.append((d, o))
         reqs = []
         for k, n in enumerate(sizes):
             g = sdfb.make_grid((-0.5,) * 3, 1.0 / n, (n, n + 1, n - 1))
@@ -25,13 +43,14 @@ def test_served_equals_plain_in_the_mix(ctx):
             o = np.empty(g.shape, np.uint8)
             reqs.append((srv.submit(ids[k % 3], g, d, o), k % 3, g, d, o))
         infos = []
-        for rid, m, g, d, o in reqs:
+        for k, (rid, m, g, d, o) in enumerate(reqs):
             done, info = srv.poll(rid, 60000)
             assert done and info["status"] == 0
             infos.append(info)
+            if k < 3:  # the same request in a mixed wave: bit-identical to it alone
+                assert np.array_equal(d, alone[k][0]) and np.array_equal(o, alone[k][1])
             d1, o1 = ctx.bake(*meshes[m], g, sdfb.make_opts())
-            assert np.array_equal(o, o1)
-            assert np.array_equal(d, d1)
+            assert_same_bake(d, o, d1, o1)
         assert all(i["t_submit_ms"] <= i["t_admit_ms"] <= i["t_done_ms"] for i in infos)
 
 
@@ -48,7 +67,7 @@ def test_served_gwn_mesh(ctx):
         done, info = srv.poll(rid, 60000)
         assert done
     d1, o1 = ctx.bake(v, f, g, sdfb.make_opts())
-    assert np.array_equal(o, o1) and np.array_equal(d, d1)
+    assert_same_bake(d, o, d1, o1)
 
 
 def test_budget_evicts_least_recently_used(ctx):
@@ -86,7 +105,7 @@ def test_pinned_outputs(ctx):
         rid = srv.submit(srv.register(v, f), g, d, o)
         assert srv.poll(rid, 60000)[0]
     d1, o1 = ctx.bake(v, f, g, sdfb.make_opts())
-    assert np.array_equal(d, d1) and np.array_equal(o, o1)
+    assert_same_bake(d, o, d1, o1)
 
 
 def test_concurrent_registration_of_the_same_mesh(ctx):
@@ -127,7 +146,7 @@ def test_concurrent_registration_of_the_same_mesh(ctx):
     assert len(results) == 16
     for m, done, status, d, o in results:
         assert done and status == 0
-        assert np.array_equal(d, ref[m][0]) and np.array_equal(o, ref[m][1])
+        assert_same_bake(d, o, ref[m][0], ref[m][1])
 
 
 def test_admission_evicts_and_always_progresses(ctx):
@@ -148,7 +167,7 @@ def test_admission_evicts_and_always_progresses(ctx):
             done, info = srv.poll(srv.submit(b, g, d, o), 60000)
             assert done and info["status"] == 0
             d1, o1 = ctx.bake(*ms[1], g, sdfb.make_opts())
-            assert np.array_equal(d, d1) and np.array_equal(o, o1)
+            assert_same_bake(d, o, d1, o1)
         del a
 
 
