@@ -464,7 +464,9 @@ sdfb_status sdfb_bake_soup(sdfb_ctx *ctx, const float *positions, uint32_t num_t
   p.V = V;
   p.T = num_tris;
   p.grid = *grid_out;
-  p.dist = want_dist ? static_cast<float *>(ctx->out_dist.p) : nullptr;
+  float *const direct_dist =
+      (want_dist && p.sign != kSignGwn) ? static_cast<float *>(mapped_host(dist_out)) : nullptr;
+  p.dist = want_dist ? (direct_dist ? direct_dist : static_cast<float *>(ctx->out_dist.p)) : nullptr;
   p.occ = want_occ ? static_cast<uint8_t *>(ctx->out_occ.p) : nullptr;
   if (p.sign == kSignGwn && want_dist) {
     // the caps are built on the host from the welded mesh
@@ -484,7 +486,8 @@ sdfb_status sdfb_bake_soup(sdfb_ctx *ctx, const float *positions, uint32_t num_t
   }
   s = run_batch(ctx, st, ms, o, false, stats);
   if (s != SDFB_OK) return s;
-  if (want_dist) CK(cudaMemcpyAsync(dist_out, ctx->out_dist.p, cells * 4, cudaMemcpyDeviceToHost, st));
+  if (want_dist && !direct_dist)
+    CK(cudaMemcpyAsync(dist_out, ctx->out_dist.p, cells * 4, cudaMemcpyDeviceToHost, st));
   if (want_occ) CK(cudaMemcpyAsync(occ_out, ctx->out_occ.p, cells, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   return SDFB_OK;

@@ -333,15 +333,19 @@ class Context:
                                        C.byref(stats) if stats is not None else None)
         self._check(st)
 
-    def bake_soup(self, positions, bmin, bmax, resolution: int, opts: Opts | None = None, stats: Stats | None = None):
+    def bake_soup(self, positions, bmin, bmax, resolution: int, opts: Opts | None = None, stats: Stats | None = None,
+                  alloc=None):
+        """The reference's bakeSdf(MeshAsset, resolution): returns (grid, dist, occ). `alloc(shape,
+        dtype)` may supply the output arrays (pinned ones are written in place)."""
         p = _f32(positions).reshape(-1, 3)
         g = GridDesc()
         st = self.lib.sdfb_bake_soup(self.h, _ptr(p), len(p) // 3, _ptr(_f32(bmin)), _ptr(_f32(bmax)),
                                      int(resolution), C.byref(opts) if opts is not None else None, C.byref(g), None,
                                      None, None)
         self._check(st)
-        dist = np.empty(g.shape, np.float32)
-        occ = np.empty(g.shape, np.uint8)
+        alloc = alloc or (lambda shape, dtype: np.empty(shape, dtype))
+        dist = alloc(g.shape, np.float32)
+        occ = alloc(g.shape, np.uint8)
         st = self.lib.sdfb_bake_soup(self.h, _ptr(p), len(p) // 3, _ptr(_f32(bmin)), _ptr(_f32(bmax)),
                                      int(resolution), C.byref(opts) if opts is not None else None, C.byref(g),
                                      _ptr(dist), _ptr(occ), C.byref(stats) if stats is not None else None)

@@ -130,3 +130,12 @@ def test_pinned_outputs_are_written_in_place(ctx):
     hd.fill(np.nan)
     ctx.bake(v, f, g, opts, out=(hd, ho))
     assert np.array_equal(hd, d1) and np.array_equal(ho, o1)
+    # the reference-shaped soup entry point
+    soup = v[f.reshape(-1)].reshape(-1, 3)
+    lo, hi = soup.min(axis=0), soup.max(axis=0)
+    g0, d0, o0 = ctx.bake_soup(soup, lo, hi, 40, opts)
+    tdt = {np.float32: torch.float32, np.uint8: torch.uint8}
+    g2, d2, o2 = ctx.bake_soup(soup, lo, hi, 40, opts,
+                               alloc=lambda shape, dt: torch.empty(int(np.prod(shape)), dtype=tdt[dt])
+                               .pin_memory().numpy().reshape(shape))
+    assert g2.shape == g0.shape and np.array_equal(d2, d0) and np.array_equal(o2, o0)
