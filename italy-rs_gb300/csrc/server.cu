@@ -17,8 +17,9 @@
 //     requests; waves run on separate streams, so a wave admitted while others are on the GPU
 //     overlaps with them. Each cell is computed exactly as in a single bake, so a result is the
 //     same alone and in any mix.
-//   * Outputs go straight to the caller's buffers when they are pinned (cudaMemcpyAsync), else
-//     through the wave's pinned staging buffer and a host copy when the wave retires.
+//   * Outputs go straight to the caller's buffers when they are pinned (a pinned distance grid is
+//     written in place by the distance kernel, occupancy by cudaMemcpyAsync), else through the
+//     wave's pinned staging buffer and a host copy when the wave retires.
 //   * sdfb_poll waits (bounded) on a condition variable for a request's completion.
 #include <algorithm>
 #include <chrono>
@@ -88,6 +89,7 @@ struct Request {
   float *dist_out = nullptr;
   uint8_t *occ_out = nullptr;
   bool dist_pinned = false, occ_pinned = false;
+  float *dist_direct = nullptr;  // device address of a pinned distance output the wave writes in place
   double t_submit = 0, t_admit = 0, t_done = 0;
   int status = -1;  // -1 pending, else sdfb_status
   uint64_t voxels = 0;
@@ -119,6 +121,18 @@ bool is_pinned(const void *p) {
     return false;
   }
   return a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged;
+}
+
+// The device address of page-locked host memory, or null (the distance kernel then writes the
+// request's grid in place over NVLink-C2C).
+float *mapped_host(float *p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? static_cast<float *>(a.devicePointer) : nullptr;
 }
 
 }  // namespace
@@ -254,7 +268,11 @@ bool sdfb_server::launch_wave(Wave &w) {
     }
     p.bvh = &m->tree;
     p.grid = r->grid;
-    p.dist = r->dist_out ? static_cast<float *>(w.out_dist.p) + w.offs[k] : nullptr;
+    // A pinned distance output is written in place, except for winding-number meshes, whose band
+    // pass reads the distances back.
+    r->dist_direct = (r->dist_pinned && m->sign != kSignGwn) ? mapped_host(r->dist_out) : nullptr;
+    p.dist = r->dist_out ? (r->dist_direct ? r->dist_direct : static_cast<float *>(w.out_dist.p) + w.offs[k])
+                         : nullptr;
     p.occ = r->occ_out ? static_cast<uint8_t *>(w.out_occ.p) + w.offs[k] : nullptr;
     plan.push_back(p);
   }
@@ -272,11 +290,12 @@ bool sdfb_server::launch_wave(Wave &w) {
 
 // Copies each request's grids out of the wave buffers: straight into pinned caller buffers,
 // through the wave's pinned staging buffer otherwise (finished by retire_wave on the host).
+// Distances already written in place need no copy.
 void enqueue_readback(Wave &w) {
   for (size_t k = 0; k < w.reqs.size(); ++k) {
     Request *r = w.reqs[k];
     const uint64_t n = uint64_t(r->grid.nx) * r->grid.ny * r->grid.nz;
-    if (r->dist_out) {
+    if (r->dist_out && !r->dist_direct) {
       const float *src = static_cast<const float *>(w.out_dist.p) + w.offs[k];
       void *dst = r->dist_pinned ? static_cast<void *>(r->dist_out)
                                  : static_cast<void *>(static_cast<float *>(w.stage_dist.p) + w.offs[k]);
