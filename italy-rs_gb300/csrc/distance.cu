@@ -13,14 +13,14 @@
 // Two passes keep one expensive tile from holding the whole GPU. Cells far inside a closed surface
 // are nearly equidistant to much of it, so their tiles walk a large part of the tree; a single
 // such tile, taken late by one warp, used to run alone for a quarter of the kernel. In pass A a
-// walk looks at the tile counter every `step_budget` steps; once every tile has been handed out
+// walk looks at the chunk counter every `step_budget` steps; once every chunk has been handed out
 // (the tail, where a long walk would keep one SM busy while the rest idle) it stops, stores its
 // cells' current bounds (squared distances, upper bounds of the answer) in the output and appends
-// the tile to a deferred list. Pass B
-// gives each deferred tile a whole block: the tree is cut into 2^kSplitBits subtrees below the
-// root, the block's warps take subtrees from a shared counter, each walks its subtree for all the
-// tile's cells starting from the stored bounds, and the warps publish their bounds to shared
-// memory (atomicMin on the float bits, valid for non-negative values) after every subtree.
+// the tile to a deferred list. Pass B gives each deferred tile a whole block: the tree is cut into
+// 2^kSplitBits subtrees below the root, the block's warps take subtrees from a shared counter,
+// each walks its subtree for all the tile's cells starting from the stored bounds, and the warps
+// publish their bounds to shared memory (atomicMin on the float bits, valid for non-negative
+// values) after every subtree.
 //
 // Sign: parity counts the column's crossing heights above each cell (the crossing list is
 // built by parity.cu). Winding-number signs are applied afterwards by gwn.cu, which needs the
@@ -37,7 +37,7 @@ namespace {
 
 // Pass A: a block takes chunks of consecutive tiles (a brick of neighbouring tiles) and its warps
 // take tiles from the block's chunk, so the warps sharing an SM's L1 walk overlapping parts of the
-// tree. 10 warps fill the register file twice over at the ~92 registers of the 4-cells-per-lane
+// tree. 10 warps fill the register file twice over at the 96 registers of the 4-cells-per-lane
 // tiles (20 warps per SM). Pass B's block shares one tile: 16 warps over 64 subtrees, which also
 // keeps a small grid (fewer tiles than the GPU holds warps) busy once its tiles are deferred.
 constexpr int kThreadsA = 320;
