@@ -347,7 +347,8 @@ def percentile(xs, p):
     return ys[k]
 
 
-def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, repeat=0.3, workers=48):
+def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, repeat=0.3, workers=64,
+                 wave_log2=27, max_inflight=64):
     """The Poisson serving stream. Returns the served record and the request list (for plain)."""
     import numpy as np
     rng = np.random.default_rng(seed)
@@ -373,7 +374,7 @@ def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, re
         slot_bufs.append((d, o))
         slots.put(k)
     results = [None] * len(reqs)
-    srv = sdfb.Server(ctx, hbm_budget_bytes=150 << 30, max_inflight=64, wave_voxels_log2=25)
+    srv = sdfb.Server(ctx, hbm_budget_bytes=150 << 30, max_inflight=max_inflight, wave_voxels_log2=wave_log2)
     mesh_cache = {}
     lock = threading.Lock()
     work = queue.Queue()

@@ -156,7 +156,7 @@ struct sdfb_server {
   uint64_t next_req = 1, tick = 0;
   uint64_t budget = 0, resident_bytes_used = 0, inflight_bytes = 0;
   int max_inflight = 64, inflight = 0;
-  uint64_t wave_cells = 1ull << 25;
+  uint64_t wave_cells = 1ull << 27;
   std::string err;
   cudaMemPool_t pool = nullptr;
 
@@ -438,7 +438,7 @@ sdfb_status sdfb_server_create(sdfb_ctx *ctx, const sdfb_server_opts *opts, sdfb
   cudaMemGetInfo(&free_b, &total_b);
   srv->budget = o.hbm_budget_bytes ? o.hbm_budget_bytes : uint64_t(free_b) * 3 / 4;
   srv->max_inflight = o.max_inflight > 0 ? o.max_inflight : 64;
-  srv->wave_cells = 1ull << (o.wave_voxels_log2 > 10 && o.wave_voxels_log2 < 36 ? o.wave_voxels_log2 : 25);
+  srv->wave_cells = 1ull << (o.wave_voxels_log2 > 10 && o.wave_voxels_log2 < 36 ? o.wave_voxels_log2 : 27);
   srv->sched = make_private_ctx(ctx->device, ctx->num_sms, ctx);
   if (!srv->sched) return SDFB_ERR_CUDA;
   for (int k = 0; k < kRegSlots; ++k) {
