@@ -113,7 +113,8 @@ typedef struct sdfb_stats {
   uint64_t tiles_deferred;  /* distance tiles that exceeded the step budget and were finished by a
                                whole block in the second distance pass */
   uint64_t plane_tests;     /* count_work: cell-plane lower-bound tests (lanes) that screen triangles */
-  uint64_t reserved[2];
+  uint64_t rect_tests;      /* count_work: in-plane bounding-rectangle tests (lanes) after the plane screen */
+  uint64_t reserved[1];
 } sdfb_stats;
 
 /* ---- context ---------------------------------------------------------------------------- */

@@ -88,7 +88,7 @@ struct GwnInput {
 // Workspace::misc (256 bytes, zeroed before every bake): error flags at 0, the distance tile
 // counter at 64, work counters at 128 (box, triangle, SAT, plane tests), the deferral counters at
 // 160.
-constexpr size_t kMiscDeferOffset = 160;
+constexpr size_t kMiscDeferOffset = 192;
 // Traversal steps a distance tile may take before it is deferred to the block-per-tile pass.
 constexpr int kDefaultStepBudget = 1024;
 

@@ -228,12 +228,15 @@ struct DistTri {
   float4 q0, q1, q2, q3, q4;
 };
 
-// Squared distance from (u, v) to the 2D triangle (0, 0), (b, 0), (c1, c2) of a DistTri (q4 holds
-// the edge projection factors). Branch-free: every lane executes the same instructions.
-__device__ __forceinline__ float inplane_dist2(float u, float v, float b, float c1, float c2, float bc,
+// Distance from u to [0, b] (edge AB's extent on the u axis).
+__device__ __forceinline__ float dist_to_range(float u, float b) { return fmaxf(fmaxf(-u, u - b), 0.0f); }
+
+// Squared distance from (u, v) to the 2D triangle (0, 0), (b, 0), (c1, c2) of a DistTri, given
+// du = dist_to_range(u, b) (q4 holds the edge projection factors). Branch-free: every lane
+// executes the same instructions.
+__device__ __forceinline__ float inplane_dist2(float u, float v, float du, float b, float c1, float c2, float bc,
                                                const float4 &k) {
-  const float du = u - fminf(fmaxf(u, 0.0f), b);  // edge AB on the u axis
-  const float d_ab = fmaf(du, du, v * v);
+  const float d_ab = fmaf(du, du, v * v);  // edge AB on the u axis
   const float s1 = __saturatef(fmaf(v, k.y, u * k.x));  // edge AC
   const float x1 = fmaf(-s1, c1, u), y1 = fmaf(-s1, c2, v);
   const float d_ac = fmaf(x1, x1, y1 * y1);
@@ -298,10 +301,12 @@ __device__ inline DistTri make_dist_tri(float3 fa, float3 fb, float3 fc) {
 // FP32 arithmetic of the distance tests, counted as flops (add / sub / mul = 1, FMA = 2; min, max,
 // saturate and compares are not counted), for the roofline figure. Per cell and triangle:
 // plane bound = 3 (ap) + 5 (h = ap . e_h) + 1 (h^2)                                          =  9
-// full test   = 2 x 5 (u, v) + 4 (edge AB) + 10 (edge AC) + 11 (edge BC) + 6 (inside) + 1     = 42
-//               (on top of the plane bound, whose ap, h and h^2 it reuses)
+// rectangle   = 2 x 5 (u, v) + 2 (u - b, v - c2) + 4 (du^2 + dv^2 + h^2)                     = 16
+// full test   = 3 (edge AB) + 10 (edge AC) + 11 (edge BC) + 6 (inside) + 1                     = 31
+//               (each stage on top of the ones before, whose values it reuses)
 // box_dist2   = 3 x 2 (sub) + 5 (|d|^2)                                                      = 11
-constexpr int kFlopsPointTri = 42;
+constexpr int kFlopsPointTri = 31;
+constexpr int kFlopsPointRect = 16;
 constexpr int kFlopsPointBox = 11;
 constexpr int kFlopsPointPlane = 9;
 

@@ -59,7 +59,7 @@ constexpr Shape kShapes[] = {{4, 4, 2}, {8, 4, 1}, {4, 4, 4}, {8, 4, 2}, {4, 4, 
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
 struct WalkStats {
-  unsigned long long box_tests = 0, tri_tests = 0, plane_tests = 0;
+  unsigned long long box_tests = 0, tri_tests = 0, plane_tests = 0, rect_tests = 0;
   bool overflow = false, corrupt = false;
 };
 
@@ -139,12 +139,25 @@ __device__ __forceinline__ void test_leaf(const DistTri *__restrict__ tris, int 
     }
     if (COUNT) ws.plane_tests += kWarp * VPL;
     if (!__any_sync(kFull, need)) continue;
+    // Then the distance to the triangle's bounding rectangle in its own plane, [0, b] x [0, c2],
+    // with h^2: much tighter where a cell is near the triangle's plane but beside the triangle
+    // (most cells that pass the plane bound). Its u part is edge AB's clamp in the full test.
     const float su = fmaf(ay, q1.y, ax * q1.x), sv = fmaf(ay, q2.y, ax * q2.x);
+    float u[VPL], w[VPL], du[VPL];
+    need = false;
 #pragma unroll
     for (int v = 0; v < VPL; ++v) {
-      const float u = fmaf(az[v], q1.z, su), w = fmaf(az[v], q2.z, sv);
-      best[v] = fminf(best[v], h2[v] + inplane_dist2(u, w, q0.w, q1.w, q2.w, q3.w, q4));
+      u[v] = fmaf(az[v], q1.z, su);
+      w[v] = fmaf(az[v], q2.z, sv);
+      du[v] = dist_to_range(u[v], q0.w);
+      const float dw = dist_to_range(w[v], q2.w);
+      need |= fmaf(du[v], du[v], fmaf(dw, dw, h2[v])) < best[v];
     }
+    if (COUNT) ws.rect_tests += kWarp * VPL;
+    if (!__any_sync(kFull, need)) continue;
+#pragma unroll
+    for (int v = 0; v < VPL; ++v)
+      best[v] = fminf(best[v], h2[v] + inplane_dist2(u[v], w[v], du[v], q0.w, q1.w, q2.w, q3.w, q4));
     if (COUNT) ws.tri_tests += kWarp * VPL;
   }
 }
@@ -303,6 +316,7 @@ __device__ __forceinline__ void flush_stats(const DistanceArgs &a, const WalkSta
     atomicAdd(a.work_counters, ws.box_tests);
     atomicAdd(a.work_counters + 1, ws.tri_tests);
     atomicAdd(a.work_counters + 3, ws.plane_tests);
+    atomicAdd(a.work_counters + 4, ws.rect_tests);
   }
 }
 

@@ -149,7 +149,7 @@ struct DistanceArgs {
   uint32_t *err;
   unsigned long long *tile_counter;   // pass A's chunk counter, zeroed by the launcher
   unsigned long long chunk_tiles;     // tiles per chunk (set by the launcher)
-  unsigned long long *work_counters;  // optional: [0] box, [1] triangle, [3] plane tests (lanes)
+  unsigned long long *work_counters;  // optional: [0] box, [1] triangle, [3] plane, [4] rectangle tests (lanes)
   // Deferral of long tiles (none when defer_list is null or step_budget <= 0): every step_budget
   // traversal steps a walk checks whether all tiles have been handed out and, if so, defers its
   // tile. The list holds defer_capacity tile indices; defer_counters[0] counts deferred tiles (it

@@ -551,14 +551,15 @@ sdfb_status finish_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, const Ba
     sv.ms_distance = ms_d;
     sv.voxels = S.total_cells;
     sv.triangles = S.total_tris;
-    unsigned long long w[4] = {0, 0, 0, 0};
+    unsigned long long w[5] = {0, 0, 0, 0, 0};
     cudaMemcpy(w, d_work, sizeof w, cudaMemcpyDeviceToHost);
     sv.box_tests = w[0];
     sv.tri_tests = w[1];
     sv.sat_tests = w[2];
     sv.plane_tests = w[3];
-    sv.flops_distance =
-        double(w[0]) * kFlopsPointBox + double(w[1]) * kFlopsPointTri + double(w[3]) * kFlopsPointPlane;
+    sv.rect_tests = w[4];
+    sv.flops_distance = double(w[0]) * kFlopsPointBox + double(w[1]) * kFlopsPointTri +
+                        double(w[3]) * kFlopsPointPlane + double(w[4]) * kFlopsPointRect;
     if (S.any_cross)
       cudaMemcpy(&sv.crossings, static_cast<uint64_t *>(ws.col_start.p) + S.total_cols, 8, cudaMemcpyDeviceToHost);
     if (S.any_gwn) cudaMemcpy(&sv.gwn_fp64_cells, gwn_refine_counter(ws.gwn_tmp.p), 8, cudaMemcpyDeviceToHost);

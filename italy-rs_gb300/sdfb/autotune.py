@@ -32,7 +32,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 DEFAULT_OUT = os.path.join(os.path.dirname(HERE), "tuning", "gb300.tsv")
 
 TILES = (1, 2, 3, 4, 5, 6)
-LEAVES = (1, 2, 3, 4, 6, 8)
+LEAVES = (1, 2, 3, 4, 6, 8, 12, 16)
 STACKS = (32, 64)
 BUDGETS = (-1, 32, 128, 512, 1024, 2048, 4096)
 START = (4, 3, 64, 1024)  # leaf, tile id (1-based), stack, step budget: the built-in defaults
