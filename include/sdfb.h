@@ -82,8 +82,22 @@ typedef struct sdfb_opts {
   int32_t step_budget;    /* a distance tile's walk checks every this many steps whether all tiles
                              are handed out, and if so leaves its tile to a second pass where a
                              whole block finishes it; 0: autotuned table, -1: never */
-  int32_t reserved[6];
+  int32_t fault_inject;   /* testing only, 0 in normal use: SDFB_FAULT_* bits that make a bounded
+                             device wait or limit run out on purpose (the bake then fails with the
+                             status that limit maps to, and the context stays usable) */
+  int32_t alloc_cap_kib;  /* testing only, 0 = none: a workspace allocation above this many KiB
+                             fails as if the device were out of memory (SDFB_ERR_OUT_OF_MEMORY) */
+  int32_t reserved[4];
 } sdfb_opts;
+
+/* sdfb_opts.fault_inject bits. None of them faults the GPU: each makes a wait or a limit that the
+ * kernels already bound run out early, so the error path behind it can be tested. */
+#define SDFB_FAULT_DISPATCH 1      /* no warp hands its block a new chunk of distance tiles: the
+                                      other warps' bounded wait for one runs out -> INTERNAL */
+#define SDFB_FAULT_STEP_LIMIT 2    /* a traversal walk may take only 8 steps -> INTERNAL */
+#define SDFB_FAULT_SHALLOW_STACK 4 /* a 32-entry traversal stack holds 2 entries: the walk
+                                      overflows and the bake reruns with 64 entries */
+#define SDFB_FAULT_STACK_ALL 8     /* every traversal stack holds 2 entries -> OVERFLOW */
 
 /* Per-call statistics, filled when the pointer is non-null. Times are CUDA-event times on the
  * bake stream (ms); counts are exact. */
@@ -331,12 +345,14 @@ const char *sdfb_server_last_error(const sdfb_server *srv);
  * allocator and cudaFree's device-wide synchronisation. All buffers are device memory supplied by
  * the caller;
  * work is enqueued on `stream` (a cudaStream_t, NULL = the legacy default stream) and not waited
- * for. Working memory is one fixed device array inside the library (about 12 MiB, held on every
+ * for. Working memory is one fixed device array inside the library (about 16 MiB, held on every
  * device that loads the library until the process exits), so:
  *   - meshes above 1,048,576 triangles are rejected with SDFB_ERR_INVALID_ARGUMENT;
  *   - the first call on each device sets up the array's address and must come before any stream
  *     capture on that device;
- *   - calls whose work overlaps on the GPU share the array and race; order them on one stream. */
+ *   - calls whose work overlaps on the GPU share the array and race; order them on one stream;
+ *   - launch failures are read with cudaGetLastError, which also clears an error left pending by
+ *     the caller's own earlier work on this host thread: check your own errors first. */
 sdfb_status sdfb_occupancy_noalloc(const float *d_verts, uint32_t num_verts, const uint32_t *d_idx,
                                    uint32_t num_tris, const sdfb_grid_desc *grid, uint8_t *d_occ_out,
                                    void *stream);

@@ -6,9 +6,31 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/sdfb.h"
 #include "kernels.h"
+
+// NVTX range in the "sdfb" domain for one bake stage (build, occupancy, crossings, distance,
+// winding number, ...): a profiler attributes the kernels launched inside it to the stage. The
+// header-only NVTX3 API costs a branch when no tool is attached.
+inline nvtxDomainHandle_t nvtx_domain() {
+  static const nvtxDomainHandle_t d = nvtxDomainCreateA("sdfb");
+  return d;
+}
+struct NvtxRange {
+  explicit NvtxRange(const char *name) {
+    nvtxEventAttributes_t a = {};
+    a.version = NVTX_VERSION;
+    a.size = NVTX_EVENT_ATTRIB_STRUCT_SIZE;
+    a.messageType = NVTX_MESSAGE_TYPE_ASCII;
+    a.message.ascii = name;
+    nvtxDomainRangePushEx(nvtx_domain(), &a);
+  }
+  ~NvtxRange() { nvtxDomainRangePop(nvtx_domain()); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Grow-only device buffer.
 struct DevBuf {

@@ -18,6 +18,9 @@ enum DevErr : uint32_t {
   kErrDispatch = 64u,         // a block's tile dispatch waited past its limit
 };
 
+// sdfb_opts.fault_inject bits as the kernels see them (include/sdfb.h, SDFB_FAULT_*).
+enum FaultBits : int { kFaultDispatch = 1, kFaultStepLimit = 2, kFaultShallowStack = 4, kFaultStackAll = 8 };
+
 constexpr int kWarp = 32;
 constexpr uint32_t kFull = 0xffffffffu;
 

@@ -175,14 +175,31 @@ struct TailCheck {
 // distances; inactive cells hold -1 and never ask for work). Returns false when the walk stopped
 // early by the tail check with work left (best[] then holds upper bounds); a walk past the limit a
 // correct tree allows stops with the corrupt flag.
+// Bounds of one walk: the step limit (a correct tree expands each inner node at most once per walk
+// and pops at most once per push) and the usable stack entries. The fault-injection bits shrink
+// them so that the error paths behind them can be tested.
+struct WalkLimits {
+  int steps, stack;
+};
+template <int STACK>
+__device__ __forceinline__ WalkLimits walk_limits(int num_nodes, int fault) {
+  WalkLimits l;
+  l.steps = num_nodes > (INT_MAX - 64) / 2 ? INT_MAX - 1 : 2 * num_nodes + 64;
+  l.stack = STACK;
+  if (fault) {
+    if (fault & kFaultStepLimit) l.steps = 8;
+    if ((fault & kFaultStackAll) || (STACK == 32 && (fault & kFaultShallowStack))) l.stack = 2;
+  }
+  return l;
+}
+
 template <int VPL, int STACK, bool COUNT>
 __device__ __forceinline__ bool walk(const Node *__restrict__ nodes, const DistTri *__restrict__ tris, int num_nodes,
-                                     int num_tris, int start, TailCheck tail, int lane, float tcx, float tcy,
-                                     float tcz, float px, float py, const float (&pz)[VPL], float (&best)[VPL],
-                                     WalkStats &ws) {
+                                     int num_tris, int start, TailCheck tail, WalkLimits lim, int lane, float tcx,
+                                     float tcy, float tcz, float px, float py, const float (&pz)[VPL],
+                                     float (&best)[VPL], WalkStats &ws) {
   static_assert(STACK == 32 || STACK == 64, "stack depth is one or two registers per lane");
-  // A correct tree expands each inner node at most once per walk and pops at most once per push.
-  const int step_limit = num_nodes > (INT_MAX - 64) / 2 ? INT_MAX - 1 : 2 * num_nodes + 64;
+  const int step_limit = lim.steps;
   int next_check = tail.every > 0 ? tail.every : INT_MAX;
   int cur = start, sp = 0, stk0 = 0, stk1 = 0;
   for (int steps = 0;; ++steps) {
@@ -252,7 +269,7 @@ __device__ __forceinline__ bool walk(const Node *__restrict__ nodes, const DistT
     if (near_w && near_cnt == 0) {
       cur = near_ref;
       if (far_w) {
-        if (sp < STACK) {
+        if (sp < lim.stack) {
           const int e = (node << 1) | (second_first ? 0 : 1);
           if (STACK == 32 || sp < 32) {
             if (lane == sp) stk0 = e;
@@ -327,7 +344,10 @@ __device__ __forceinline__ void flush_stats(const DistanceArgs &a, const WalkSta
 // every chunk has been handed out.
 __device__ unsigned long long next_tile(unsigned long long *state, unsigned long long *chunks,
                                         unsigned long long per_chunk, unsigned long long total_chunks,
-                                        unsigned long long total_tiles, uint32_t *err) {
+                                        unsigned long long total_tiles, uint32_t *err, int fault) {
+  // Fault injection: nobody moves the block on, and the waits are short.
+  const bool stuck = fault & kFaultDispatch;
+  const int spin_limit = stuck ? (1 << 12) : kDispatchSpin;
   for (;;) {
     const unsigned long long old = atomicAdd(state, 1ull);
     const unsigned long long chunk = old >> 32, idx = old & 0xffffffffull;
@@ -337,14 +357,14 @@ __device__ unsigned long long next_tile(unsigned long long *state, unsigned long
       if (t < total_tiles) return t;
       continue;  // past the end of the last chunk: draw on until the block moves on
     }
-    if (idx == per_chunk) {
+    if (idx == per_chunk && !stuck) {
       atomicExch(state, atomicAdd(chunks, 1ull) << 32);
       continue;
     }
     const volatile unsigned long long *vs = state;
     int spin = 0;
-    while ((*vs >> 32) == chunk && spin < kDispatchSpin) ++spin;
-    if (spin == kDispatchSpin) {
+    while ((*vs >> 32) == chunk && spin < spin_limit) ++spin;
+    if (spin == spin_limit) {
       atomic_or_err(err, kErrDispatch);
       return kNoTile;
     }
@@ -370,7 +390,8 @@ __global__ __launch_bounds__(kThreadsA) void k_distance(DistanceArgs a) {
 
   for (;;) {
     unsigned long long tile = 0;
-    if (lane == 0) tile = next_tile(&s_state, a.tile_counter, a.chunk_tiles, total_chunks, B.total_tiles, a.err);
+    if (lane == 0)
+      tile = next_tile(&s_state, a.tile_counter, a.chunk_tiles, total_chunks, B.total_tiles, a.err, a.fault);
     tile = __shfl_sync(kFull, tile, 0);
     if (tile == kNoTile) break;
     Cells c;
@@ -379,8 +400,9 @@ __global__ __launch_bounds__(kThreadsA) void k_distance(DistanceArgs a) {
     float best[VPL];
 #pragma unroll
     for (int v = 0; v < VPL; ++v) best[v] = c.active[v] ? kInf : -1.0f;
-    bool done = walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, M.root, tail, lane, c.cx, c.cy,
-                                        c.cz, c.px, c.py, c.pz, best, ws);
+    const WalkLimits lim = walk_limits<STACK>(M.bvh_nodes, a.fault);
+    bool done = walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, M.root, tail, lim, lane, c.cx,
+                                        c.cy, c.cz, c.px, c.py, c.pz, best, ws);
     if (!done) {
       unsigned long long slot = 0;
       if (lane == 0) slot = atomicAdd(a.defer_counters, 1ull);
@@ -393,8 +415,8 @@ __global__ __launch_bounds__(kThreadsA) void k_distance(DistanceArgs a) {
         continue;
       }
       // The list is full: finish the tile here, from the bounds found so far.
-      walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, M.root, never, lane, c.cx, c.cy, c.cz, c.px,
-                              c.py, c.pz, best, ws);
+      walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, M.root, never, lim, lane, c.cx, c.cy, c.cz,
+                              c.px, c.py, c.pz, best, ws);
     }
     store_cells<TX, TY, TZ>(a, c, best);
   }
@@ -487,8 +509,9 @@ __global__ __launch_bounds__(kThreads) void k_distance_deferred(DistanceArgs a) 
         cur = ref;
       }
       if (walk_it)
-        walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, cur, TailCheck{nullptr, 0, 0}, lane, c.cx,
-                                c.cy, c.cz, c.px, c.py, c.pz, best, ws);
+        walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, cur, TailCheck{nullptr, 0, 0},
+                                walk_limits<STACK>(M.bvh_nodes, a.fault), lane, c.cx, c.cy, c.cz, c.px, c.py, c.pz,
+                                best, ws);
 #pragma unroll
       for (int v = 0; v < VPL; ++v)
         if (c.active[v]) atomicMin(&s_best[v * kWarp + lane], __float_as_uint(best[v]));

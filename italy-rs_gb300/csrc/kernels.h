@@ -32,6 +32,8 @@ struct Scratch {
 // hold n + 1 values. Scratch need: scan_scratch_bytes(n).
 size_t scan_scratch_bytes(size_t n);
 cudaError_t exclusive_scan_u32(const uint32_t *in, uint64_t *out, size_t n, Scratch s, cudaStream_t st);
+// The same for uint64 counts (per-triangle candidate counts, which can pass 2^32 on large grids).
+cudaError_t exclusive_scan_u64(const uint64_t *in, uint64_t *out, size_t n, Scratch s, cudaStream_t st);
 
 // Stable LSD radix sort of (key, value) pairs on bits [0, bits) of the keys, 8 bits per pass.
 // keys/vals hold the input and receive the result; keys_alt/vals_alt are same-size temporaries.
@@ -159,6 +161,7 @@ struct DistanceArgs {
   unsigned long long defer_capacity;
   unsigned long long *defer_counters;
   long long step_budget;
+  int fault;  // sdfb_opts.fault_inject bits (testing only; 0 in normal use)
 };
 
 int tile_shape_count();

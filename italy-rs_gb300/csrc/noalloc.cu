@@ -8,7 +8,9 @@
 // allocator's unbounded time. This entry point serves them: it runs the same occupancy kernels
 // as the context-based bake, but its working memory -- per-triangle candidate counts, their scan and
 // the one-mesh batch record -- lives in a fixed file-scope device array, so a call allocates
-// nothing. The caller passes device inputs and the device output grid.
+// nothing. The caller passes device inputs and the device output grid. The one-mesh record is
+// written into the array by a one-thread kernel that receives it as a launch argument, so no
+// host memory is read after the call returns.
 //
 // Limits and rules:
 //   * at most kNoAllocMaxTris triangles; larger meshes are rejected with
@@ -20,7 +22,9 @@
 //   * every call shares the one array: calls whose work overlaps on the GPU (different streams,
 //     or different host threads without ordering) race on it. Nothing in it has to start at zero:
 //     each call writes the counts and records it reads, and the occupancy grid is cleared by the
-//     call itself.
+//     call itself;
+//   * launch failures are read with cudaGetLastError, which also clears an error that the
+//     caller's own earlier work left pending on this host thread.
 #include <cstring>
 #include <mutex>
 
@@ -34,15 +38,28 @@ namespace {
 
 constexpr uint32_t kNoAllocMaxTris = 1u << 20;  // 1,048,576 triangles
 constexpr size_t kRecordBytes = 4096;           // one MeshRec and its prefix tables
-// Candidate counts (4 B per triangle), their exclusive scan (8 B per triangle + 1), the scan's
-// block sums, plus alignment slack: about 12 MiB in all.
-constexpr size_t kScratchBytes = kRecordBytes + size_t(kNoAllocMaxTris) * 12 + (size_t(1) << 16);
+// Candidate counts (8 B per triangle), their exclusive scan (8 B per triangle + 1), the scan's
+// block sums, plus alignment slack: about 16 MiB in all.
+constexpr size_t kScratchBytes = kRecordBytes + size_t(kNoAllocMaxTris) * 16 + (size_t(1) << 16);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 void *g_scratch_addr[kMaxDevices] = {};
+
+// The one-mesh batch record and its prefix tables.
+struct Records {
+  MeshRec rec;
+  alignas(8) uint64_t tris[2];
+  alignas(8) uint64_t cells[2];
+  alignas(8) uint64_t zero[2];
+};
+static_assert(sizeof(Records) <= kRecordBytes, "records fit their slot");
+static_assert(sizeof(Records) <= 4000, "records pass as one kernel argument");
+
+// Writes the records into the array; the argument is copied when the launch is enqueued.
+__global__ void k_put_records(Records *dst, Records src) { *dst = src; }
 
 }  // namespace
 
@@ -73,33 +90,21 @@ extern "C" sdfb_status sdfb_occupancy_noalloc(const float *d_verts, uint32_t num
     scratch = g_scratch_addr[dev];
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  // The one-mesh batch record and its prefix tables, written into the first kRecordBytes.
-  MeshRec r;
-  std::memset(&r, 0, sizeof r);
-  r.verts = d_verts;
-  r.idx = d_idx;
-  r.num_verts = num_verts;
-  r.num_tris = num_tris;
-  r.occ = d_occ_out;
-  r.g = to_dev(*grid);
-  r.leaf_size = 1;
   const uint64_t cells = uint64_t(grid->nx) * grid->ny * grid->nz;
-  struct Records {
-    MeshRec rec;
-    alignas(8) uint64_t tris[2];
-    alignas(8) uint64_t cells[2];
-    alignas(8) uint64_t zero[2];
-  } h;
-  static_assert(sizeof(Records) <= kRecordBytes, "records fit their slot");
+  Records h;
   std::memset(&h, 0, sizeof h);
-  h.rec = r;
+  h.rec.verts = d_verts;
+  h.rec.idx = d_idx;
+  h.rec.num_verts = num_verts;
+  h.rec.num_tris = num_tris;
+  h.rec.occ = d_occ_out;
+  h.rec.g = to_dev(*grid);
+  h.rec.leaf_size = 1;
   h.tris[1] = num_tris;
   h.cells[1] = cells;
   char *d = static_cast<char *>(scratch);
-  if (cudaMemcpyAsync(d, &h, sizeof h, cudaMemcpyHostToDevice, st) != cudaSuccess) {
-    cudaGetLastError();
-    return SDFB_ERR_CUDA;
-  }
+  k_put_records<<<1, 1, 0, st>>>(reinterpret_cast<Records *>(d), h);
+  if (cudaGetLastError() != cudaSuccess) return SDFB_ERR_CUDA;
   const Records *dr = reinterpret_cast<const Records *>(d);
   BatchDev B;
   B.num_meshes = 1;

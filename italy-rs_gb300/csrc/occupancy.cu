@@ -62,7 +62,9 @@ __device__ __forceinline__ TriCells tri_cells(const BatchDev &B, uint64_t t) {
   return r;
 }
 
-__global__ __launch_bounds__(kThreads) void k_occ_items(BatchDev B, uint32_t *__restrict__ items) {
+// Candidate cells per triangle, as 64-bit counts: one triangle across a large grid can have more
+// than 2^32 candidate cells.
+__global__ __launch_bounds__(kThreads) void k_occ_items(BatchDev B, uint64_t *__restrict__ items) {
   const uint64_t t = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
   if (t >= B.total_tris) return;
   const TriCells tc = tri_cells(B, t);
@@ -70,9 +72,7 @@ __global__ __launch_bounds__(kThreads) void k_occ_items(BatchDev B, uint32_t *__
     items[t] = 0;
     return;
   }
-  const uint64_t n = uint64_t(tc.hi[0] - tc.lo[0] + 1) * uint64_t(tc.hi[1] - tc.lo[1] + 1) *
-                     uint64_t(tc.hi[2] - tc.lo[2] + 1);
-  items[t] = n > 0xffffffffull ? 0xffffffffu : static_cast<uint32_t>(n);
+  items[t] = uint64_t(tc.hi[0] - tc.lo[0] + 1) * uint64_t(tc.hi[1] - tc.lo[1] + 1) * uint64_t(tc.hi[2] - tc.lo[2] + 1);
 }
 
 // Clears the occupancy grids of the batch (one pass over the global cells).
@@ -158,7 +158,7 @@ __global__ __launch_bounds__(kThreads) void k_occ_test(BatchDev B, const uint64_
 }
 
 struct OccTemp {
-  uint32_t *items;
+  uint64_t *items;
   uint64_t *starts;
   void *scratch;
   size_t scratch_bytes;
@@ -172,7 +172,7 @@ size_t occ_layout(uint64_t T, char *base, OccTemp *o) {
     return p;
   };
   OccTemp x;
-  x.items = reinterpret_cast<uint32_t *>(take(size_t(T) * 4 + 4));
+  x.items = reinterpret_cast<uint64_t *>(take(size_t(T) * 8 + 8));
   x.starts = reinterpret_cast<uint64_t *>(take((size_t(T) + 1) * 8));
   x.scratch_bytes = scan_scratch_bytes(T);
   x.scratch = take(x.scratch_bytes);
@@ -202,7 +202,7 @@ cudaError_t occupancy_batch(const BatchDev &B, uint32_t *first_tri, void *temp, 
   if (occ_layout(T, static_cast<char *>(temp), &o) > temp_bytes) return cudaErrorMemoryAllocation;
   k_occ_items<<<static_cast<unsigned>((T + kThreads - 1) / kThreads), kThreads, 0, st>>>(B, o.items);
   note_launch();
-  if ((e = exclusive_scan_u32(o.items, o.starts, T, Scratch{o.scratch, o.scratch_bytes}, st)) != cudaSuccess) return e;
+  if ((e = exclusive_scan_u64(o.items, o.starts, T, Scratch{o.scratch, o.scratch_bytes}, st)) != cudaSuccess) return e;
   if (first_tri)
     k_occ_test<true, false><<<num_sms * 8, kThreads, 0, st>>>(B, o.starts, first_tri, sat_tests, HitSink());
   else
@@ -227,7 +227,7 @@ cudaError_t occupancy_hits(const BatchDev &B, void *temp, size_t temp_bytes, uin
   if (occ_layout(T, static_cast<char *>(temp), &o) > temp_bytes) return cudaErrorMemoryAllocation;
   k_occ_items<<<static_cast<unsigned>((T + kThreads - 1) / kThreads), kThreads, 0, st>>>(B, o.items);
   note_launch();
-  if ((e = exclusive_scan_u32(o.items, o.starts, T, Scratch{o.scratch, o.scratch_bytes}, st)) != cudaSuccess) return e;
+  if ((e = exclusive_scan_u64(o.items, o.starts, T, Scratch{o.scratch, o.scratch_bytes}, st)) != cudaSuccess) return e;
   HitSink sink;
   sink.keys = keys;
   sink.capacity = capacity;

@@ -33,9 +33,13 @@ using namespace sdfb;
     if (e_ != cudaSuccess) return ctx_cuda(ctx, e_, #call); \
   } while (0)
 
+// A test-only cap on single workspace allocations (sdfb_opts.alloc_cap_kib), set per bake on the
+// calling thread: an allocation above it fails as cudaMalloc would when the device is full.
+thread_local uint64_t t_alloc_cap = 0;
+
 #define ENSURE(buf, bytes)                                                                       \
   do {                                                                                           \
-    if (!(buf).ensure(bytes))                                                                    \
+    if ((t_alloc_cap && static_cast<uint64_t>(bytes) > t_alloc_cap) || !(buf).ensure(bytes))     \
       return ctx_fail(ctx, SDFB_ERR_OUT_OF_MEMORY, "cannot allocate %zu bytes of device memory", \
                       static_cast<size_t>(bytes));                                               \
   } while (0)
@@ -354,6 +358,7 @@ sdfb_status enqueue_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, std::ve
   for (const auto &p : ms)
     if ((p.bvh != nullptr) != (ms[0].bvh != nullptr))
       return ctx_fail(ctx, SDFB_ERR_INTERNAL, "a batch mixes resident and unbuilt meshes");
+  t_alloc_cap = o.alloc_cap_kib > 0 ? uint64_t(o.alloc_cap_kib) << 10 : 0;
   Layout L;
   make_layout(ctx, ms, o, L);
   const int M = static_cast<int>(ms.size());
@@ -417,6 +422,7 @@ sdfb_status enqueue_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, std::ve
   da.defer_capacity = defer_cap;
   da.defer_counters = reinterpret_cast<unsigned long long *>(static_cast<char *>(ws.misc.p) + kMiscDeferOffset);
   da.step_budget = L.step_budget;
+  da.fault = o.fault_inject;
   GwnInput gi;
   gi.batch = B;
   gi.col_start = static_cast<const uint64_t *>(ws.col_start.p);
@@ -433,22 +439,42 @@ sdfb_status enqueue_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, std::ve
   };
   auto enqueue = [&]() -> sdfb_status {
     CK(rec(ws.ev[6]));
-    CK(cudaMemcpyAsync(ws.batch_buf.p, ws.staging.p, L.bytes, cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(ws.misc.p, 0, 256, st));
+    {
+      NvtxRange r("sdfb prepare");
+      CK(cudaMemcpyAsync(ws.batch_buf.p, ws.staging.p, L.bytes, cudaMemcpyHostToDevice, st));
+      CK(cudaMemsetAsync(ws.misc.p, 0, 256, st));
+    }
     CK(rec(ws.ev[0]));
-    if (build) CK(lbvh_build(B, bvh, ws.build_tmp.p, ws.build_tmp.cap, d_err, st));
+    if (build) {
+      NvtxRange r("sdfb build");
+      CK(lbvh_build(B, bvh, ws.build_tmp.p, ws.build_tmp.cap, d_err, st));
+    }
     CK(rec(ws.ev[1]));
-    if (any_occ) CK(occupancy_batch(B, nullptr, ws.build_tmp.p, ws.build_tmp.cap, d_sat, ctx->num_sms, st));
+    if (any_occ) {
+      NvtxRange r("sdfb occupancy");
+      CK(occupancy_batch(B, nullptr, ws.build_tmp.p, ws.build_tmp.cap, d_sat, ctx->num_sms, st));
+    }
     CK(rec(ws.ev[2]));
-    if (S.any_cross)
+    if (S.any_cross) {
+      NvtxRange r("sdfb crossings");
       CK(parity_columns(B, static_cast<uint64_t *>(ws.col_start.p), static_cast<float *>(ws.col_z.p),
                         static_cast<int8_t *>(ws.col_s.p), S.capacity, ws.par_tmp.p, ws.par_tmp.cap, d_err,
                         ctx->num_sms, st));
-    if (K > 0) CK(lbvh_build(CB, caps, ws.caps_tmp.p, ws.caps_tmp.cap, d_err, st));
+    }
+    if (K > 0) {
+      NvtxRange r("sdfb caps build");
+      CK(lbvh_build(CB, caps, ws.caps_tmp.p, ws.caps_tmp.cap, d_err, st));
+    }
     CK(rec(ws.ev[3]));
-    CK(distance_launch(da, L.tile_id, L.stack, ctx->num_sms, st));
+    {
+      NvtxRange r("sdfb distance");
+      CK(distance_launch(da, L.tile_id, L.stack, ctx->num_sms, st));
+    }
     CK(rec(ws.ev[4]));
-    if (S.any_gwn) CK(gwn_enqueue(gi, ws.gwn_tmp.p, ctx->num_sms, st));
+    if (S.any_gwn) {
+      NvtxRange r("sdfb winding number");
+      CK(gwn_enqueue(gi, ws.gwn_tmp.p, ctx->num_sms, st));
+    }
     CK(rec(ws.ev[5]));
     return SDFB_OK;
   };
@@ -463,7 +489,7 @@ sdfb_status enqueue_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, std::ve
                           ws.caps_tmp.p,  ws.gwn_tmp.p, ws.defer.p, static_cast<void *>(st)};
     const uint64_t extra[] = {uint64_t(L.tile_id), uint64_t(L.stack), S.capacity, L.bytes, ws.build_tmp.cap,
                               ws.par_tmp.cap, ws.caps_tmp.cap, uint64_t(o.band_voxels * 1e6f),
-                              uint64_t(L.step_budget), defer_cap};
+                              uint64_t(L.step_budget), defer_cap, uint64_t(uint32_t(o.fault_inject))};
     key.insert(key.end(), reinterpret_cast<const uint8_t *>(ptrs), reinterpret_cast<const uint8_t *>(ptrs) + sizeof ptrs);
     key.insert(key.end(), reinterpret_cast<const uint8_t *>(extra),
                reinterpret_cast<const uint8_t *>(extra) + sizeof extra);
@@ -523,7 +549,8 @@ sdfb_status finish_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, const Ba
   }
   if (h_err & kErrStackOverflow)
     return ctx_fail(ctx, SDFB_ERR_OVERFLOW, "BVH traversal stack overflow (depth > %d)", S.stack);
-  if (h_err & kErrCorruptTree) return ctx_fail(ctx, SDFB_ERR_INTERNAL, "BVH walk met an invalid reference");
+  if (h_err & kErrCorruptTree)
+    return ctx_fail(ctx, SDFB_ERR_INTERNAL, "BVH walk met an invalid reference or ran past its step limit");
   if (h_err & kErrDispatch) return ctx_fail(ctx, SDFB_ERR_INTERNAL, "distance tile dispatch timed out");
   if (stats) {
     sdfb_stats sv;

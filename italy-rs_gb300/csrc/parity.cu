@@ -71,12 +71,13 @@ __device__ __forceinline__ TriCols tri_cols(const BatchDev &B, uint64_t t) {
   return r;
 }
 
-__global__ __launch_bounds__(kThreads) void k_col_items(BatchDev B, uint32_t *__restrict__ items) {
+// Candidate columns per triangle, as 64-bit counts (a triangle across a wide, flat grid can cover
+// more than 2^32 columns).
+__global__ __launch_bounds__(kThreads) void k_col_items(BatchDev B, uint64_t *__restrict__ items) {
   const uint64_t t = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
   if (t >= B.total_ptris) return;
   const TriCols tc = tri_cols(B, t);
-  const uint64_t n = uint64_t(tc.x1 - tc.x0 + 1) * uint64_t(tc.y1 - tc.y0 + 1);
-  items[t] = tc.x1 < tc.x0 ? 0u : (n > 0xffffffffull ? 0xffffffffu : static_cast<uint32_t>(n));
+  items[t] = tc.x1 < tc.x0 ? 0ull : uint64_t(tc.x1 - tc.x0 + 1) * uint64_t(tc.y1 - tc.y0 + 1);
 }
 
 template <bool FILL>
@@ -126,7 +127,7 @@ __global__ __launch_bounds__(kThreads) void k_col_hits(BatchDev B, const uint64_
 }
 
 struct ParTemp {
-  uint32_t *items;
+  uint64_t *items;
   uint64_t *starts;
   uint32_t *col_count;
   void *scratch;
@@ -141,7 +142,7 @@ size_t par_layout(uint64_t T, uint64_t ncols, char *base, ParTemp *o) {
     return p;
   };
   ParTemp x;
-  x.items = reinterpret_cast<uint32_t *>(take(size_t(T) * 4 + 4));
+  x.items = reinterpret_cast<uint64_t *>(take(size_t(T) * 8 + 8));
   x.starts = reinterpret_cast<uint64_t *>(take((size_t(T) + 1) * 8));
   x.col_count = reinterpret_cast<uint32_t *>(take(ncols * 4 + 4));
   x.scratch_bytes = std::max(scan_scratch_bytes(T), scan_scratch_bytes(ncols));
@@ -167,7 +168,7 @@ cudaError_t parity_columns(const BatchDev &B, uint64_t *col_start, float *col_z,
   const Scratch sc{o.scratch, o.scratch_bytes};
   k_col_items<<<static_cast<unsigned>((T + kThreads - 1) / kThreads), kThreads, 0, st>>>(B, o.items);
   note_launch();
-  if ((e = exclusive_scan_u32(o.items, o.starts, T, sc, st)) != cudaSuccess) return e;
+  if ((e = exclusive_scan_u64(o.items, o.starts, T, sc, st)) != cudaSuccess) return e;
   const unsigned grid = num_sms * 8;
   k_col_hits<false><<<grid, kThreads, 0, st>>>(B, o.starts, o.col_count, nullptr, nullptr, nullptr, 0, err);
   note_launch();

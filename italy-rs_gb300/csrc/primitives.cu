@@ -203,6 +203,11 @@ cudaError_t exclusive_scan_u32(const uint32_t *in, uint64_t *out, size_t n, Scra
   return scan_impl<uint32_t>(in, out, n, b, st);
 }
 
+cudaError_t exclusive_scan_u64(const uint64_t *in, uint64_t *out, size_t n, Scratch s, cudaStream_t st) {
+  Bump b{static_cast<char *>(s.ptr), s.bytes};
+  return scan_impl<uint64_t>(in, out, n, b, st);
+}
+
 size_t sort_scratch_bytes(size_t n) {
   const size_t ntiles = (n + kSortTile - 1) / kSortTile;
   const size_t cells = ntiles * 256;

@@ -26,6 +26,12 @@ ERR_NOT_FOUND = 8
 ERR_NO_DEVICE = 9
 ERR_INTERNAL = 10
 
+# sdfb_opts.fault_inject bits (testing only; see include/sdfb.h)
+FAULT_DISPATCH = 1
+FAULT_STEP_LIMIT = 2
+FAULT_SHALLOW_STACK = 4
+FAULT_STACK_ALL = 8
+
 SIGN_AUTO, SIGN_PARITY, SIGN_GWN, SIGN_NONE = 0, 1, 2, 3
 
 
@@ -52,7 +58,8 @@ class Opts(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("sign_mode", C.c_int32), ("band_voxels", C.c_float),
                 ("leaf_size", C.c_int32), ("tile", C.c_int32), ("no_occupancy", C.c_int32),
                 ("no_distance", C.c_int32), ("count_work", C.c_int32), ("stack_depth", C.c_int32),
-                ("step_budget", C.c_int32), ("reserved", C.c_int32 * 6)]
+                ("step_budget", C.c_int32), ("fault_inject", C.c_int32), ("alloc_cap_kib", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
 
 class Stats(C.Structure):
@@ -218,9 +225,10 @@ def make_grid(origin, voxel, n) -> GridDesc:
 
 def make_opts(sign_mode: int = SIGN_AUTO, band_voxels: float = 1.0, leaf_size: int = 0, tile: int = 0,
               no_occupancy: bool = False, no_distance: bool = False, count_work: bool = False,
-              stack_depth: int = 0, step_budget: int = 0) -> Opts:
+              stack_depth: int = 0, step_budget: int = 0, fault_inject: int = 0, alloc_cap_kib: int = 0) -> Opts:
     """tile: shape 1..6 (0 = tuned); leaf_size 1..16 (0 = tuned); stack_depth 32 or 64 (0 = tuned);
-    step_budget: traversal steps before a distance tile is deferred (0 = tuned, -1 = never)."""
+    step_budget: traversal steps before a distance tile is deferred (0 = tuned, -1 = never);
+    fault_inject / alloc_cap_kib: testing only (FAULT_* bits; a workspace allocation cap)."""
     o = Opts()
     o.struct_size = C.sizeof(Opts)
     o.sign_mode = sign_mode
@@ -232,6 +240,8 @@ def make_opts(sign_mode: int = SIGN_AUTO, band_voxels: float = 1.0, leaf_size: i
     o.count_work = int(count_work)
     o.stack_depth = stack_depth
     o.step_budget = step_budget
+    o.fault_inject = fault_inject
+    o.alloc_cap_kib = alloc_cap_kib
     return o
 
 

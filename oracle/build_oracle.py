@@ -6,8 +6,9 @@
   triangle/box test header, ``voxelize.cpp``, ``mesh_weld.cpp`` and ``mesh_validate.cpp`` --
   where they lie in the reference tree, against the small glm stand-in in
   ``oracle/glm_shim``, together with ``oracle/ref_driver.cpp``, into
-  ``oracle/_ref/libitaly_ref.so``. It needs the reference tree (``ITALY_REF_ROOT``, default
-  ``/root/reference``) and is skipped when that tree is absent.
+  ``oracle/_ref/libitaly_ref.so``. It needs the reference tree: ``ITALY_REF_ROOT`` names it, else
+  a ``reference`` folder beside this repository's root is used; without either the step is
+  skipped (the prebuilt library, if any, is kept).
 
 Both use ``-ffp-contract=off``: FP32 occupancy must round exactly as the reference does.
 """
@@ -22,7 +23,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD_DIR, "liboracle.so")
 REF_SO = os.path.join(REF_DIR, "libitaly_ref.so")
-REF_ROOT = os.environ.get("ITALY_REF_ROOT", "/root/reference")
+REF_ROOT = os.environ.get("ITALY_REF_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 REF_SOURCES = [
     "src/convert/voxelize.cpp",

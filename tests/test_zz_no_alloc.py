@@ -40,6 +40,30 @@ def test_noalloc_occupancy_matches_bake_twice(ctx):
         assert np.array_equal(docc.cpu().numpy().reshape(g.shape), ref)
 
 
+def test_noalloc_at_the_triangle_limit_on_a_caller_stream(ctx):
+    """A mesh of exactly 1,048,576 triangles (the documented maximum) on a non-blocking stream the
+    caller created: the array must hold its counts and their scan, and the result must equal the
+    context bake's, bit for bit."""
+    torch = pytest.importorskip("torch")
+    import sdfb
+    from sdfb import meshgen as mg
+    lib = sdfb.load()
+    v, f = mg.displaced_torus(1024, 512, 0.3, 0.12, 21)
+    assert len(f) == 1 << 20
+    g = sdfb.make_grid((-0.5,) * 3, 1.0 / 96, (96, 96, 96))
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        dv, di = _dev(torch, v, np.float32), _dev(torch, f.astype(np.int32), np.int32)
+        docc = torch.full((g.cells,), 3, dtype=torch.uint8, device="cuda")
+    st = lib.sdfb_occupancy_noalloc(C.c_void_p(dv.data_ptr()), len(v), C.c_void_p(di.data_ptr()), len(f),
+                                    C.byref(g), C.c_void_p(docc.data_ptr()), C.c_void_p(s.cuda_stream))
+    assert st == sdfb.OK
+    s.synchronize()
+    _, ref = ctx.bake(v, f, g, sdfb.make_opts(sign_mode=sdfb.SIGN_NONE), want_dist=False)
+    assert ref.any()
+    assert np.array_equal(docc.cpu().numpy().reshape(g.shape), ref)
+
+
 def test_noalloc_rejects_oversized_mesh(ctx):
     import sdfb
     lib = sdfb.load()
