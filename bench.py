@@ -2,7 +2,7 @@
 """Benchmark of the GB300 mesh -> SDF bake.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload batch64|displaced-sphere-256] [--serve-seconds S] [--no-serve]
+                    [--workload batch64|c1|c2|c3] [--serve-seconds S] [--no-serve] [--no-configs]
 
 Workloads (seeded synthetic meshes generated in-process; no dataset is involved):
 
@@ -12,8 +12,21 @@ Workloads (seeded synthetic meshes generated in-process; no dataset is involved)
   build, one persistent distance launch over every mesh's tiles, replayed from a CUDA graph).
   ``value`` is voxels/s of that step with meshes and outputs in HBM; ``plain`` times the same 64
   meshes through 64 single-mesh calls (sdfb_bake_device) in the same run.
-* ``displaced-sphere-256``: the level-6 displaced icosphere (81,920 triangles) on a 256^3 grid, one
-  single-mesh bake per step.
+* ``c1``: the plain-bake UV sphere (r 0.4, 64 x 32 segments, 4,096 triangles, 128 of them degenerate
+  at the poles) on a 64^3 grid, parity sign.
+* ``c2`` (alias ``displaced-sphere-256``): the level-6 displaced icosphere (81,920 triangles) on a
+  256^3 grid, parity sign.
+* ``c3``: the 500k-triangle soup (displaced spheres and tori, 2% of faces deleted) on a 512^3 grid,
+  FP32 distance, winding-number sign with FP64 inside the one-voxel band.
+  For c1-c3 a step is one single-mesh bake (through the batch entry point, a batch of one).
+
+The default line also carries ``configs``: for c1, c2 and c3 the single-mesh GPU bake time and
+voxels/s (device buffers, and end to end from host buffers), max and RMS distance error over the
+grid diagonal against the FP64 oracle (every cell for c1 and c2; for c3 the cells within 1.5 voxels
+of the surface plus a seeded uniform sample of 10^6 cells), out-of-band sign mismatches (exact
+parity on every cell; for c3 the FP64 winding number summed directly over every triangle on 4,096
+uniform cells), occupancy mismatches on every cell, and the CPU bake of the same mesh timed in the
+same run. ``batch_classes`` times the batch's meshes grouped by grid size, plain against batched.
 
 Also reported: ``served`` -- a Poisson stream (200 requests/s for --serve-seconds, default 60) of
 meshes drawn as in batch64 (30% of requests repeat an earlier mesh, the rest bring a new one) fed
@@ -60,11 +73,15 @@ def parse(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="batch64", choices=["batch64", "displaced-sphere-256"])
+    ap.add_argument("--workload", default="batch64", choices=["batch64", "c1", "c2", "c3", "displaced-sphere-256"])
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args(argv)
+    ap.add_argument("--no-configs", action="store_true")
+    a = ap.parse_args(argv)
+    if a.workload == "displaced-sphere-256":
+        a.workload = "c2"
+    return a
 
 
 _T0 = time.monotonic()
@@ -113,6 +130,33 @@ def sphere256():
     from sdfb import meshgen as mg
     v, i = mg.displaced_sphere_mesh(seed=1234)
     return v, i, 256
+
+
+CONFIG_NAMES = {
+    "c1": "plain-bake UV sphere (4,096 triangles, 128 degenerate), 64^3, parity",
+    "c2": "displaced icosphere level 6 (81,920 triangles), 256^3, parity",
+    "c3": "500k-triangle soup (2% of faces deleted), 512^3, FP32 distance + winding number (FP64 band)",
+}
+
+
+def config_mesh(name):
+    """(verts, idx, n, sign) of a single-mesh config."""
+    from sdfb import meshgen as mg
+    if name == "c1":
+        v, i = mg.uv_sphere_mesh(0.4, 64, 32)
+        return v, i, 64, "parity"
+    if name == "c2":
+        v, i, n = sphere256()
+        return v, i, n, "parity"
+    v, i = mg.soup_with_holes()
+    return v, i, 512, "gwn"
+
+
+def workload_meshes(name):
+    if name == "batch64":
+        return batch64_meshes(), "parity"
+    v, i, n, sign = config_mesh(name)
+    return [(v, i, n)], sign
 
 
 def unit_grid(sdfb, n):
@@ -270,28 +314,63 @@ def cpu_baseline(meshes, budget_s=20.0, seed=0, gpu_grids=None):
                       f" FP64 distance + exact parity: {orc.threads()} threads)"}
 
 
+def cpu_gwn_step(orc, ref, v, i, n, seed, n_dist=100_000, n_gwn=256):
+    """One reference-arm step on a winding-number config: (cells, estimated CPU seconds for every
+    cell) from occupancy of every cell plus sampled FP64 distance and direct winding number."""
+    import numpy as np
+    from oracle.oracle import soup_of
+    origin, voxel, dims = (-0.5, -0.5, -0.5), 1.0 / n, (n, n, n)
+    cells = n ** 3
+    rng = np.random.default_rng(seed)
+    t0 = time.perf_counter()
+    if ref is not None:
+        ref.occupancy(soup_of(v, i), origin, voxel, dims)
+    else:
+        orc.occupancy(v, i, origin, voxel, dims)
+    t_occ = time.perf_counter() - t0
+    sd = np.sort(rng.choice(cells, n_dist, replace=False)).astype(np.int64)
+    t0 = time.perf_counter()
+    orc.distance(v, i, origin, voxel, dims, samples=sd)
+    t_d = time.perf_counter() - t0
+    sw = np.sort(rng.choice(cells, n_gwn, replace=False)).astype(np.int64)
+    t0 = time.perf_counter()
+    orc.gwn(v, i, origin, voxel, dims, samples=sw)
+    t_w = time.perf_counter() - t0
+    return cells, t_occ + (t_d / n_dist + t_w / n_gwn) * cells
+
+
 def run_reference(args, rank, world):
     """The reference arm: the CPU bake of the workload (the reference's own bake of this path is an
     OptiX ray-cast estimate and the OptiX SDK is absent, so its CPU occupancy code and the FP64
     oracle stand in). Each step bakes meshes of the workload in a seeded order for a bounded time."""
     if rank != 0:
         return
-    meshes = batch64_meshes() if args.workload == "batch64" else [sphere256()]
+    meshes, sign = workload_meshes(args.workload)
     orc, ref, kind = cpu_tools()
     budget = max(5.0, min(25.0, 150.0 / max(args.steps, 1)))
-    for w in range(min(args.warmup, 1)):
-        cpu_sample(meshes, 1.0, 1000 + w, orc, ref)
     vox, secs, used = 0, 0.0, 0
-    for step in range(args.steps):
-        a, b, c = cpu_sample(meshes, budget, step, orc, ref)
-        vox, secs, used = vox + a, secs + b, used + c
+    if sign == "gwn":
+        # the 512^3 soup: each step times occupancy on every cell and distance + direct winding
+        # number on a seeded sample of cells, and counts the whole grid at that per-cell cost
+        v, i, n = meshes[0]
+        for step in range(args.steps):
+            a, b = cpu_gwn_step(orc, ref, v, i, n, step)
+            vox, secs, used = vox + a, secs + b, used + 1
+        what = "occupancy of every cell + FP64 distance on 10^5 and direct FP64 winding number on 256 sampled cells"
+    else:
+        for w in range(min(args.warmup, 1)):
+            cpu_sample(meshes, 1.0, 1000 + w, orc, ref)
+        for step in range(args.steps):
+            a, b, c = cpu_sample(meshes, budget, step, orc, ref)
+            vox, secs, used = vox + a, secs + b, used + c
+        what = f"{used} mesh bakes over {args.steps} steps of ~{budget:.0f} s, {vox} voxels"
     value = vox / secs if secs else 0.0
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": args.workload},
             "cpu_baseline": {"value": value, "unit": "voxels/s", "cores": orc.threads(), "kind": kind,
-                             "sample": f"{used} mesh bakes over {args.steps} steps of ~{budget:.0f} s, {vox} voxels"},
+                             "sample": what},
             "e2e": {"value": value, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -348,8 +427,11 @@ def percentile(xs, p):
 
 
 def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, repeat=0.3, workers=64,
-                 wave_log2=27, max_inflight=64):
-    """The Poisson serving stream. Returns the served record and the request list (for plain)."""
+                 wave_log2=27, max_inflight=64, closed_loop=False):
+    """The Poisson serving stream. Returns the served record and the request list (for plain).
+    closed_loop: no arrival times -- each of the `workers` clients submits its next request as soon
+    as its last one returns, for `seconds` (the server's capacity at that concurrency); latency is
+    then measured from submission."""
     import numpy as np
     rng = np.random.default_rng(seed)
     reqs, t, news = [], 0.0, []
@@ -394,6 +476,8 @@ def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, re
             if item is None:
                 return
             k, arrival = item
+            if closed_loop:
+                arrival = time.monotonic()
             if time.monotonic() > deadline[0]:
                 with lock:
                     dropped.append(k)
@@ -442,10 +526,10 @@ def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, re
     d0, o0 = slot_bufs[0]
     srv.poll(srv.submit(srv.register(v0, f0), g0, d0[:g0.cells], o0[:g0.cells]), 120000)
     t0 = time.monotonic()
-    deadline[0] = t0 + seconds + max(60.0, seconds)
+    deadline[0] = t0 + (seconds if closed_loop else seconds + max(60.0, seconds))
     for k, (arr, key, n) in enumerate(reqs):
         now = time.monotonic() - t0
-        if arr > now:
+        if arr > now and not closed_loop:
             time.sleep(arr - now)
         work.put((k, t0 + arr))
     for _ in threads:
@@ -500,6 +584,195 @@ def plain_stream(sdfb, ctx, base_meshes, reqs, seconds):
             "note": f"arrivals of the first {seconds:.0f} s of the same stream, one sdfb_bake per request"}
 
 
+# ---------------------------------------------------------------------------------------------
+# Per-config records (c1-c3): GPU time, FP64 precision, mismatches, CPU bake of the same mesh
+
+
+def vpl_of_tile(tile_used: int) -> int:
+    """Cells per lane of a distance tile shape (sdfb_opts.tile numbering, 1-based)."""
+    shapes = {1: (4, 4, 2), 2: (8, 4, 1), 3: (4, 4, 4), 4: (8, 4, 2), 5: (4, 4, 8), 6: (8, 4, 4)}
+    tx, ty, tz = shapes.get(int(tile_used), (4, 4, 8))
+    return tz // (32 // (tx * ty))
+
+
+def executed_flops(st) -> float:
+    """FP32 flops of the distance tests as the kernel executes them: the terms a lane forms once for
+    its VPL cells (the x and y parts of a box distance, of the plane height and of the in-plane
+    coordinates) are counted once per lane. Per cell: box 4 + 7/VPL, plane 4 + 5/VPL, rectangle
+    10 + 6/VPL, full test 31 (the counts behind sdfb_stats.flops_distance charge every cell 11, 9,
+    16 and 31)."""
+    vpl = vpl_of_tile(st.tile_used)
+    return (st.box_tests * (4 + 7 / vpl) + st.plane_tests * (4 + 5 / vpl) + st.rect_tests * (10 + 6 / vpl)
+            + st.tri_tests * 31.0)
+
+
+def gpu_single(sdfb, ctx, torch, stream, flush, v, i, n, sign, reps=5):
+    """Single-mesh bake on device buffers (sdfb_bake_device), median of `reps` timed bakes after two
+    warm-ups, plus the same bake end to end from host buffers (sdfb_bake, pinned outputs). Returns
+    (record, signed distances, occupancy) as host arrays."""
+    import numpy as np
+    g = unit_grid(sdfb, n)
+    mode = sdfb.SIGN_PARITY if sign == "parity" else sdfb.SIGN_GWN
+    opts = sdfb.make_opts(sign_mode=mode)
+    dv, di = torch.from_numpy(v).cuda(), torch.from_numpy(i.astype(np.int32)).cuda()
+    dd = torch.empty(g.cells, dtype=torch.float32, device="cuda")
+    do = torch.empty(g.cells, dtype=torch.uint8, device="cuda")
+
+    def bake(st=None):
+        ctx.bake_device(dv.data_ptr(), len(v), di.data_ptr(), len(i), g, opts, dd.data_ptr(), do.data_ptr(),
+                        stream.cuda_stream, st)
+
+    for _ in range(2):
+        bake()
+    ms, st = [], None
+    for _ in range(reps):
+        flush.fill_(1.0)
+        st = new_stats(sdfb)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        bake(st)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    hd = torch.empty(g.cells, dtype=torch.float32).pin_memory().numpy().reshape(g.shape)
+    ho = torch.empty(g.cells, dtype=torch.uint8).pin_memory().numpy().reshape(g.shape)
+    ctx.bake(v, i, g, opts, out=(hd, ho))
+    e2e = []
+    for _ in range(3):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.bake(v, i, g, opts, out=(hd, ho))
+        e2e.append(time.perf_counter() - t0)
+    med = statistics.median(ms)
+    rec = {"triangles": int(len(i)), "voxels": int(g.cells), "grid": n, "sign": sign, "gpu_ms": med,
+           "voxels_per_s": g.cells / (med * 1e-3), "e2e_ms": 1e3 * statistics.median(e2e),
+           "e2e_voxels_per_s": g.cells / statistics.median(e2e),
+           "stages_ms": {"build": st.ms_build, "occupancy": st.ms_occupancy, "sign": st.ms_sign,
+                         "distance": st.ms_distance},
+           "gwn_fp64_cells": int(st.gwn_fp64_cells) if sign == "gwn" else None}
+    gpu_d = dd.cpu().numpy().reshape(g.shape) if sign == "parity" else hd.copy()
+    gpu_o = do.cpu().numpy().reshape(g.shape)
+    if sign == "gwn":
+        gpu_o = ho.copy()
+    del dv, di, dd, do
+    return rec, gpu_d, gpu_o
+
+
+def cpu_check(name, v, i, n, sign, gpu_d, gpu_o, seed=5):
+    """The CPU bake of a config's mesh, timed, and the GPU grid's error against it. c1 and c2 are
+    baked on every cell (occupancy: the reference's own code where compiled, one thread; FP64
+    distance and exact parity: the oracle on all host threads). c3 compares every cell's
+    occupancy, FP64 distance on the cells within 1.5 voxels of the surface and on a uniform sample
+    of 10^6 cells, and the FP64 winding number summed over every triangle on 4,096 uniform cells;
+    its CPU rate is the occupancy of every cell plus distance and winding number per sampled cell,
+    scaled to the whole grid."""
+    import numpy as np
+    from oracle.oracle import soup_of
+    orc, ref, kind = cpu_tools()
+    origin, voxel, dims = (-0.5, -0.5, -0.5), 1.0 / n, (n, n, n)
+    cells = n ** 3
+    diag = math.sqrt(3.0)
+    t0 = time.perf_counter()
+    occ = ref.occupancy(soup_of(v, i), origin, voxel, dims) if ref is not None else orc.occupancy(v, i, origin, voxel, dims)
+    t_occ = time.perf_counter() - t0
+    occ_bad = int(np.count_nonzero(np.asarray(occ).reshape(-1) != gpu_o.reshape(-1)))
+    got = gpu_d.reshape(-1).astype(np.float64)
+    out = {"occupancy_mismatches": occ_bad, "occupancy_cells_compared": cells}
+    if sign == "parity":
+        t0 = time.perf_counter()
+        d64 = orc.distance(v, i, origin, voxel, dims)
+        sg = orc.sign_parity(v, i, origin, voxel, dims, axis=2)
+        t_ds = time.perf_counter() - t0
+        err = np.abs(np.abs(got) - d64) / diag
+        far = d64 > voxel
+        out.update({"max_err_over_diag": float(err.max()), "rms_err_over_diag": float(np.sqrt(np.mean(err ** 2))),
+                    "distance_cells_compared": cells, "compared": "every cell",
+                    "sign_mismatches_outside_1_voxel": int(np.count_nonzero((got[far] < 0) != (sg[far] < 0))),
+                    "sign_cells_compared": int(np.count_nonzero(far)),
+                    "sign_reference": "exact +z parity (oracle)"})
+        cpu_s = t_occ + t_ds
+        what = "every cell"
+    else:
+        rng = np.random.default_rng(seed)
+        band = np.flatnonzero(np.abs(got) <= 1.5 * voxel).astype(np.int64)
+        uni = np.sort(rng.choice(cells, 1_000_000, replace=False)).astype(np.int64)
+        t0 = time.perf_counter()
+        d_uni = orc.distance(v, i, origin, voxel, dims, samples=uni)
+        t_du = time.perf_counter() - t0
+        d_band = orc.distance(v, i, origin, voxel, dims, samples=band)
+        e_uni = np.abs(np.abs(got[uni]) - d_uni) / diag
+        e_band = np.abs(np.abs(got[band]) - d_band) / diag
+        err = np.concatenate([e_uni, e_band])
+        ws = np.sort(rng.choice(uni, 4096, replace=False)).astype(np.int64)
+        t0 = time.perf_counter()
+        w = orc.gwn(v, i, origin, voxel, dims, samples=ws)
+        t_w = time.perf_counter() - t0
+        d_ws = orc.distance(v, i, origin, voxel, dims, samples=ws)
+        far = (d_ws > voxel) & (np.abs(np.abs(w) - 0.5) > 1e-6)
+        bad = int(np.count_nonzero((got[ws][far] < 0) != (np.abs(w[far]) > 0.5)))
+        out.update({"max_err_over_diag": float(err.max()), "rms_err_over_diag": float(np.sqrt(np.mean(err ** 2))),
+                    "distance_cells_compared": int(err.size),
+                    "compared": f"{band.size} cells within 1.5 voxels of the surface + a seeded uniform sample "
+                                f"of {uni.size} cells",
+                    "sign_mismatches_outside_1_voxel": bad, "sign_cells_compared": int(np.count_nonzero(far)),
+                    "sign_reference": "FP64 winding number summed over every triangle (oracle), 4,096 uniform cells"})
+        cpu_s = t_occ + (t_du / uni.size + t_w / ws.size) * cells
+        what = (f"occupancy of every cell ({t_occ:.1f} s) + FP64 distance ({1e6 * t_du / uni.size:.2f} us/cell on "
+                f"{uni.size} cells) and direct FP64 winding number ({1e3 * t_w / ws.size:.2f} ms/cell on {ws.size} "
+                f"cells), scaled to {cells} cells")
+    out["cpu"] = {"seconds": cpu_s, "voxels_per_s": cells / cpu_s, "cores": orc.threads(), "kind": kind,
+                  "what": what + (" (occupancy: the reference's triBoxOverlap, 1 thread)" if kind == "reference"
+                                  else " (occupancy: oracle port, 1 thread)")}
+    return out
+
+
+def config_record(name, sdfb, ctx, torch, stream, flush, cpu=True):
+    v, i, n, sign = config_mesh(name)
+    rec, gd, go = gpu_single(sdfb, ctx, torch, stream, flush, v, i, n, sign)
+    rec = {"workload": CONFIG_NAMES[name], **rec}
+    if cpu:
+        rec.update(cpu_check(name, v, i, n, sign, gd, go))
+        rec["gpu_over_cpu"] = rec["voxels_per_s"] / rec["cpu"]["voxels_per_s"]
+    return rec
+
+
+def batch_classes(sdfb, ctx, torch, stream, flush, devm, grids, dptr, optr, opts, meshes, reps=3):
+    """The batch's meshes grouped by grid size: per group the plain time (one sdfb_bake_device per
+    mesh, summed) and the batched time (the group as one batch), in ms."""
+    out = {}
+    for n in sorted({m[2] for m in meshes}):
+        ks = [k for k, m in enumerate(meshes) if m[2] == n]
+
+        def plain():
+            for k in ks:
+                ctx.bake_device(devm[k][0], devm[k][1], devm[k][2], devm[k][3], grids[k], opts, dptr[k], optr[k],
+                                stream.cuda_stream)
+
+        def batched():
+            ctx.bake_batch_device([devm[k] for k in ks], [grids[k] for k in ks], opts, [dptr[k] for k in ks],
+                                  [optr[k] for k in ks], stream.cuda_stream)
+
+        res = {}
+        for label, fn in (("plain_ms", plain), ("batched_ms", batched)):
+            fn()
+            fn()
+            t = []
+            for _ in range(reps):
+                flush.fill_(1.0)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                e1.synchronize()
+                t.append(e0.elapsed_time(e1))
+            res[label] = statistics.median(t)
+        vox = sum(grids[k].cells for k in ks)
+        out[f"{n}^3"] = {"meshes": len(ks), "triangles": int(sum(len(meshes[k][1]) for k in ks)), "voxels": int(vox),
+                         **res, "batched_over_plain": res["plain_ms"] / res["batched_ms"]}
+    return out
+
+
 def main(argv=None):
     args = parse(argv)
     rank, world, local = dist_env()
@@ -527,12 +800,12 @@ def main(argv=None):
     red_max, red_sum = reducers(pg, "cuda")
 
     stage("generating meshes")
-    meshes = batch64_meshes() if args.workload == "batch64" else [sphere256()]
+    meshes, sign = workload_meshes(args.workload)
     stage(f"{len(meshes)} meshes, {sum(len(i) for _, i, _ in meshes)} triangles")
     grids = [unit_grid(sdfb, n) for _, _, n in meshes]
     cells = [g.cells for g in grids]
     total_cells = sum(cells)
-    opts = sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY)
+    opts = sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY if sign == "parity" else sdfb.SIGN_GWN)
     dev_v = [torch.from_numpy(v).cuda() for v, _, _ in meshes]
     dev_i = [torch.from_numpy(i.astype(np.int32)).cuda() for _, i, _ in meshes]
     dev_d = [torch.empty(c, dtype=torch.float32, device="cuda") for c in cells]
@@ -555,7 +828,8 @@ def main(argv=None):
     torch.cuda.synchronize()
     cst = new_stats(sdfb)
     stage("counting build")
-    step_batch(cst, sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY, count_work=True))  # counting build (untimed)
+    count_opts = sdfb.make_opts(sign_mode=opts.sign_mode, count_work=True)
+    step_batch(cst, count_opts)  # counting build (untimed)
     stage("timed steps")
 
     # ---- timed region: the batched bake ----
@@ -625,48 +899,31 @@ def main(argv=None):
             pg.destroy_process_group()
         return
 
-    # ---- the single-mesh 256^3 bake (configs' plain single-mesh GPU bake) ----
-    single = None
+    classes = None
     if args.workload == "batch64":
-        sv, si, sn = sphere256()
-        sg = unit_grid(sdfb, sn)
-        sdv, sdi = torch.from_numpy(sv).cuda(), torch.from_numpy(si.astype(np.int32)).cuda()
-        sdd = torch.empty(sg.cells, dtype=torch.float32, device="cuda")
-        sdo = torch.empty(sg.cells, dtype=torch.uint8, device="cuda")
-        for _ in range(3):
-            ctx.bake_device(sdv.data_ptr(), len(sv), sdi.data_ptr(), len(si), sg, opts, sdd.data_ptr(), sdo.data_ptr(),
-                            stream.cuda_stream)
-        ms = []
-        for _ in range(5):
-            flush.fill_(1.0)
-            st = new_stats(sdfb)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            ctx.bake_device(sdv.data_ptr(), len(sv), sdi.data_ptr(), len(si), sg, opts, sdd.data_ptr(), sdo.data_ptr(),
-                            stream.cuda_stream, st)
-            e1.record(stream)
-            e1.synchronize()
-            ms.append(e0.elapsed_time(e1))
-        single = {"workload": "displaced-sphere-256 (81,920 triangles, 256^3)", "ms": statistics.median(ms),
-                  "voxels_per_s": sg.cells / (statistics.median(ms) * 1e-3), "ms_distance": st.ms_distance,
-                  "ms_build": st.ms_build, "ms_occupancy": st.ms_occupancy, "ms_sign": st.ms_sign}
+        classes = batch_classes(sdfb, ctx, torch, stream, flush, devm, grids, dptr, optr, opts, meshes)
+        stage("grid-size classes: " + ", ".join(f"{k} {v['batched_over_plain']:.2f}x" for k, v in classes.items()))
 
-    stage("single mesh done" if single else "no single-mesh leg")
     # ---- roofline of the distance kernel ----
     peak = sgemm_peak(torch)
     stage(f"SGEMM peak {peak:.1f} TFLOP/s")
-    flops = cst.flops_distance
+    flops_count = cst.flops_distance
+    flops = executed_flops(cst)
     mean_dist_ms = statistics.mean(dist_ms)
     achieved = flops / (mean_dist_ms * 1e-3) / 1e12
     roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "traffic": None, "kernel": "k_distance (+ k_distance_deferred)", "flops_per_launch": flops,
+                "flops_per_launch_per_cell_count": flops_count,
+                "frac_per_cell_count": flops_count / (mean_dist_ms * 1e-3) / 1e12 / peak,
                 "box_tests": int(cst.box_tests), "tri_tests": int(cst.tri_tests),
-                "plane_tests": int(cst.plane_tests), "tiles_deferred": int(cst.tiles_deferred), "kernel_ms": mean_dist_ms,
+                "plane_tests": int(cst.plane_tests), "rect_tests": int(cst.rect_tests),
+                "tiles_deferred": int(cst.tiles_deferred), "tile_used": int(cst.tile_used),
+                "kernel_ms": mean_dist_ms,
                 "peak_source": "cuBLAS SGEMM 8192^3 FP32 (TF32 off), best of 5, measured in this run",
                 "algorithmic_bytes_per_launch": total_cells * 4}
     # the memory side beside it: distance writes plus one read of every mesh's hierarchy
     hbm_peak, hbm_src = hbm_peak_gbs()
-    bvh_bytes = sum(len(i) * (64 + 64) for _, i, _ in meshes)  # triangle records + nodes
+    bvh_bytes = sum(len(i) * (80 + 64) for _, i, _ in meshes)  # 80-byte triangle records + 64-byte nodes
     moved = total_cells * 4 + bvh_bytes
     roofline["hbm"] = {"bytes_per_launch": moved, "achieved_gbs": moved / (mean_dist_ms * 1e-3) / 1e9,
                        "peak_gbs": hbm_peak, "frac": moved / (mean_dist_ms * 1e-3) / 1e9 / hbm_peak,
@@ -683,17 +940,47 @@ def main(argv=None):
         served["light"] = {k: light[k] for k in ("requests", "completed", "voxels_per_s", "p50_ms", "p99_ms",
                                                  "mean_ms", "rate_per_s")}
         stage(f"light stream: p50 {light['p50_ms']:.0f} ms, p99 {light['p99_ms']:.0f} ms")
-    cpu = None if args.no_cpu_baseline else cpu_baseline(meshes, gpu_grids=hd)
-    precision = cpu.pop("precision") if cpu else None
+        sat, _ = serve_stream(sdfb, ctx, torch, meshes, min(20.0, args.serve_seconds), seed=79, rate=1000.0,
+                              closed_loop=True)
+        served["saturation"] = {k: sat[k] for k in ("requests", "completed", "dropped", "voxels_per_s", "p50_ms",
+                                                    "p99_ms", "mean_ms", "seconds")}
+        served["saturation"]["note"] = ("closed loop: 64 clients, each submits its next request when the last "
+                                        "one returns; latency from submission")
+        stage(f"saturation: {sat['voxels_per_s'] / 1e6:.0f} M voxels/s")
+
+    configs = None
+    cpu = precision = None
+    if args.workload == "batch64":
+        if not args.no_configs:
+            configs = {}
+            for name in ("c1", "c2", "c3"):
+                configs[name] = config_record(name, sdfb, ctx, torch, stream, flush, cpu=not args.no_cpu_baseline)
+                stage(f"{name}: {configs[name]['gpu_ms']:.2f} ms"
+                      + (f", max error {configs[name]['max_err_over_diag']:.3g} x diag"
+                         if 'max_err_over_diag' in configs[name] else ""))
+        cpu = None if args.no_cpu_baseline else cpu_baseline(meshes, gpu_grids=hd)
+        precision = cpu.pop("precision") if cpu else None
+    elif not args.no_cpu_baseline:
+        v, i, n, sgn = config_mesh(args.workload)
+        # the line's own grid: hd / ho from the e2e leg (a batch of one)
+        chk = cpu_check(args.workload, v, i, n, sgn, hd[0], ho[0])
+        c = chk.pop("cpu")
+        cpu = {"value": c["voxels_per_s"], "unit": "voxels/s", "cores": c["cores"], "kind": c["kind"],
+               "sample": c["what"]}
+        precision = chk
     stage("CPU baseline done" + (f": max error {precision['max_err_over_diag']:.3g} x diag" if precision else ""))
+    cfg = {"workload": args.workload, "meshes": len(meshes), "triangles": int(sum(len(i) for _, i, _ in meshes)),
+           "voxels": int(total_cells), "grids": sorted({n for _, _, n in meshes}), "sign": sign,
+           "parallelism": f"replicas x{world}",
+           "l2": "512 MB L2 flush before every timed step (outputs alone exceed L2)"}
+    cfg["seed"] = {"batch64": 2024, "c2": 1234, "c3": 4321}.get(args.workload)
+    if args.workload != "batch64":
+        cfg["description"] = CONFIG_NAMES[args.workload]
     line = {
         "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sum(step_ms) / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded meshes generated in-process)",
-        "config": {"workload": args.workload, "meshes": len(meshes), "triangles": int(sum(len(i) for _, i, _ in meshes)),
-                   "voxels": int(total_cells), "grids": sorted({n for _, _, n in meshes}), "sign": "parity",
-                   "seed": 2024 if args.workload == "batch64" else 1234, "parallelism": f"replicas x{world}",
-                   "l2": "512 MB L2 flush before every timed step (outputs alone exceed L2)"},
+        "config": cfg,
         "plain": {"value": plain_value, "unit": "voxels/s", "ms_per_step": statistics.mean(plain_ms),
                   "batched_over_plain": value / plain_value},
         "roofline": roofline,
@@ -706,7 +993,8 @@ def main(argv=None):
         "graph_replayed_steps": int(sum(replayed)),
         "precision": precision,
         "served": served,
-        "single_mesh": single,
+        "configs": configs,
+        "batch_classes": classes,
     }
     print(json.dumps(line), flush=True)
     if pg:

@@ -118,17 +118,19 @@ typedef struct sdfb_stats {
   uint64_t triangles;
   uint64_t sat_tests;      /* triangle/box tests run by the occupancy kernel */
   uint64_t crossings;      /* parity crossings found */
-  uint64_t box_tests;      /* point-box tests (lanes) when opts.count_work = 1 */
-  uint64_t tri_tests;      /* point-triangle tests (lanes) when opts.count_work = 1 */
-  double flops_distance;   /* FP32 flops of those tests (FMA = 2) */
+  uint64_t box_tests;      /* count_work: point-box tests, one per cell */
+  uint64_t tri_tests;      /* count_work: full point-triangle tests, one per cell */
+  double flops_distance;   /* count_work: FP32 flops of the distance tests as executed, terms a lane
+                              shares between its cells counted once (FMA = 2) */
   uint64_t kernel_launches; /* kernels this call launched */
   uint64_t gwn_fp64_cells;  /* GWN: cells whose winding number was evaluated in FP64 (band + ambiguous) */
   uint64_t graph_replayed;  /* 1 when the launch sequence was replayed from a CUDA graph */
   uint64_t tiles_deferred;  /* distance tiles that exceeded the step budget and were finished by a
                                whole block in the second distance pass */
-  uint64_t plane_tests;     /* count_work: cell-plane lower-bound tests (lanes) that screen triangles */
-  uint64_t rect_tests;      /* count_work: in-plane bounding-rectangle tests (lanes) after the plane screen */
-  uint64_t reserved[1];
+  uint64_t plane_tests;     /* count_work: cell-plane lower-bound tests that screen triangles, per cell */
+  uint64_t rect_tests;      /* count_work: in-plane bounding-rectangle tests after the plane screen,
+                               per cell */
+  uint64_t gwn_direct_cells; /* GWN: cells whose sign needed the direct FP64 sum over every cap */
 } sdfb_stats;
 
 /* ---- context ---------------------------------------------------------------------------- */

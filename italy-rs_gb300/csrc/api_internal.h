@@ -208,3 +208,5 @@ sdfb_status build_resident(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, const 
 size_t gwn_temp_bytes(uint64_t gwn_cells);
 cudaError_t gwn_enqueue(const GwnInput &in, void *temp, int num_sms, cudaStream_t st);
 uint64_t *gwn_refine_counter(void *temp);
+// Cells whose sign needed the direct FP64 sum over every cap triangle (the last pass).
+uint64_t *gwn_direct_counter(void *temp);

@@ -301,17 +301,22 @@ __device__ inline DistTri make_dist_tri(float3 fa, float3 fb, float3 fc) {
   return t;
 }
 
-// FP32 arithmetic of the distance tests, counted as flops (add / sub / mul = 1, FMA = 2; min, max,
-// saturate and compares are not counted), for the roofline figure. Per cell and triangle:
-// plane bound = 3 (ap) + 5 (h = ap . e_h) + 1 (h^2)                                          =  9
-// rectangle   = 2 x 5 (u, v) + 2 (u - b, v - c2) + 4 (du^2 + dv^2 + h^2)                     = 16
-// full test   = 3 (edge AB) + 10 (edge AC) + 11 (edge BC) + 6 (inside) + 1                     = 31
-//               (each stage on top of the ones before, whose values it reuses)
-// box_dist2   = 3 x 2 (sub) + 5 (|d|^2)                                                      = 11
-constexpr int kFlopsPointTri = 31;
-constexpr int kFlopsPointRect = 16;
-constexpr int kFlopsPointBox = 11;
-constexpr int kFlopsPointPlane = 9;
+// FP32 arithmetic of the distance tests as the kernel executes it, counted as flops (add / sub /
+// mul = 1, FMA = 2; min, max, saturate and compares are not counted), for the roofline figure.
+// The work counters count every test per cell; a lane forms some terms once for its VPL cells (the
+// x and y parts of a box distance, of the plane height and of the in-plane coordinates), so those
+// are spread over them. Per cell and test, each stage on top of the ones before whose values it
+// reuses:
+//   box         shared: dx 2 + dy 2 + dx^2 + dy^2 3;  per cell: dz 2 + fma 2     = 4 + 7 / VPL
+//   plane       shared: x, y offsets 2 + height 3;   per cell: z offset 1 + height 2 + h^2 1
+//                                                                                  = 4 + 5 / VPL
+//   rectangle   shared: u, v 6;  per cell: u, v 4 + range offsets 2 + sum of squares 4
+//                                                                                  = 10 + 6 / VPL
+//   full test   edge AB 3 + edge AC 10 + edge BC 11 + inside 6 + sum 1             = 31
+__host__ __device__ inline double distance_flops(int vpl, double box, double plane, double rect, double full) {
+  const double k = vpl > 0 ? 1.0 / vpl : 1.0;
+  return (4.0 + 7.0 * k) * box + (4.0 + 5.0 * k) * plane + (10.0 + 6.0 * k) * rect + 31.0 * full;
+}
 
 // ---------------------------------------------------------------------------------------------
 // BVH node (64 bytes): the boxes of both children plus their references, so one 64-byte read

@@ -5,7 +5,7 @@
 // z) taken from its block's chunk of neighbouring tiles, so long and short tiles balance across the
 // persistent grid. The warp walks the BVH together: at each node every lane measures its cells
 // against both child boxes, __any_sync decides whether any cell still needs a child, and the child
-// whose box is nearer the tile's centre goes first. Leaves are tested right away by
+// whose box centre is nearer the tile's centre goes first. Leaves are tested right away by
 // all lanes on the same triangle record (a broadcast 80-byte load), so lanes never diverge. The
 // deferred child is pushed as (node, child) and its box is re-tested against the tightened
 // bounds when popped. The stack lives in registers, one entry per lane, read with __shfl_sync.
@@ -37,10 +37,13 @@ namespace {
 
 // Pass A: a block takes chunks of consecutive tiles (a brick of neighbouring tiles) and its warps
 // take tiles from the block's chunk, so the warps sharing an SM's L1 walk overlapping parts of the
-// tree. 10 warps fill the register file twice over at the 96 registers of the 4-cells-per-lane
-// tiles (20 warps per SM). Pass B's block shares one tile: 16 warps over 64 subtrees, which also
-// keeps a small grid (fewer tiles than the GPU holds warps) busy once its tiles are deferred.
-constexpr int kThreadsA = 320;
+// tree. Two blocks of 16 warps per SM: the walk waits on dependent node and record loads, and 32
+// resident warps hide more of that latency than 20 warps without spills did (64-mesh batch
+// 281 -> 259 ms; 24 warps at 80 registers: 267 ms). Pass B's block shares one tile: 16 warps over
+// 64 subtrees, which also keeps a small grid (fewer tiles than the GPU holds warps) busy once its
+// tiles are deferred.
+constexpr int kThreadsA = 512;
+constexpr int kMinBlocksA = 2;  // 32 warps per SM: 64 registers a thread, some of them spilled to L1
 constexpr int kWarpsPerBlockA = kThreadsA / kWarp;
 // Tile order within a mesh: bricks of kBrickX x kBrickY x kBrickZ tiles, x fastest inside a brick
 // and across bricks. Tiles of a partial brick beyond the grid have no active cell.
@@ -143,21 +146,22 @@ __device__ __forceinline__ void test_leaf(const DistTri *__restrict__ tris, int 
     // with h^2: much tighter where a cell is near the triangle's plane but beside the triangle
     // (most cells that pass the plane bound). Its u part is edge AB's clamp in the full test.
     const float su = fmaf(ay, q1.y, ax * q1.x), sv = fmaf(ay, q2.y, ax * q2.x);
-    float u[VPL], w[VPL], du[VPL];
+    // The in-plane coordinates are formed again by the full test (about one screen in eight
+    // passes), so they need not stay live across the vote.
     need = false;
 #pragma unroll
     for (int v = 0; v < VPL; ++v) {
-      u[v] = fmaf(az[v], q1.z, su);
-      w[v] = fmaf(az[v], q2.z, sv);
-      du[v] = dist_to_range(u[v], q0.w);
-      const float dw = dist_to_range(w[v], q2.w);
-      need |= fmaf(du[v], du[v], fmaf(dw, dw, h2[v])) < best[v];
+      const float du = dist_to_range(fmaf(az[v], q1.z, su), q0.w);
+      const float dw = dist_to_range(fmaf(az[v], q2.z, sv), q2.w);
+      need |= fmaf(du, du, fmaf(dw, dw, h2[v])) < best[v];
     }
     if (COUNT) ws.rect_tests += kWarp * VPL;
     if (!__any_sync(kFull, need)) continue;
 #pragma unroll
-    for (int v = 0; v < VPL; ++v)
-      best[v] = fminf(best[v], h2[v] + inplane_dist2(u[v], w[v], du[v], q0.w, q1.w, q2.w, q3.w, q4));
+    for (int v = 0; v < VPL; ++v) {
+      const float u = fmaf(az[v], q1.z, su), w = fmaf(az[v], q2.z, sv);
+      best[v] = fminf(best[v], h2[v] + inplane_dist2(u, w, dist_to_range(u, q0.w), q0.w, q1.w, q2.w, q3.w, q4));
+    }
     if (COUNT) ws.tri_tests += kWarp * VPL;
   }
 }
@@ -259,9 +263,12 @@ __device__ __forceinline__ bool walk(const Node *__restrict__ nodes, const DistT
     if (COUNT) ws.box_tests += 2 * kWarp * VPL;
     w0 = __any_sync(kFull, w0) && n3.z >= 0;
     w1 = __any_sync(kFull, w1) && n3.w >= 0;
-    // Near child first: the one whose box is nearer the tile's centre (the same on every lane).
-    const bool second_first = box_dist2(tcx, tcy, tcz, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w) <
-                              box_dist2(tcx, tcy, tcz, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
+    // Near child first: the one whose box centre is nearer the tile's centre (the same on every
+    // lane). The centres order the children where the tile lies inside both boxes, as near the
+    // top of the tree; the box distances tie there (3-7% fewer tests than ordering by them).
+    const float q0x = tcx - n0.x, q0y = tcy - n0.y, q0z = tcz - n0.z;
+    const float q1x = tcx - n1.z, q1y = tcy - n1.w, q1z = tcz - n2.x;
+    const bool second_first = q1x * q1x + q1y * q1y + q1z * q1z < q0x * q0x + q0y * q0y + q0z * q0z;
     const int near_ref = second_first ? n3.y : n3.x, near_cnt = second_first ? n3.w : n3.z;
     const int far_ref = second_first ? n3.x : n3.y, far_cnt = second_first ? n3.z : n3.w;
     bool near_w = second_first ? w1 : w0, far_w = second_first ? w0 : w1;
@@ -374,7 +381,7 @@ __device__ unsigned long long next_tile(unsigned long long *state, unsigned long
 // Pass A: warps take tiles from their block's chunk, blocks take chunks from a global counter; a
 // tile still walking in the pass's tail (every chunk handed out) is deferred to pass B.
 template <int TX, int TY, int TZ, int STACK, bool COUNT>
-__global__ __launch_bounds__(kThreadsA) void k_distance(DistanceArgs a) {
+__global__ __launch_bounds__(kThreadsA, kMinBlocksA) void k_distance(DistanceArgs a) {
   using Cells = TileCells<TX, TY, TZ>;
   constexpr int VPL = Cells::VPL;
   const int lane = threadIdx.x & 31;
@@ -394,15 +401,37 @@ __global__ __launch_bounds__(kThreadsA) void k_distance(DistanceArgs a) {
       tile = next_tile(&s_state, a.tile_counter, a.chunk_tiles, total_chunks, B.total_tiles, a.err, a.fault);
     tile = __shfl_sync(kFull, tile, 0);
     if (tile == kNoTile) break;
+    // Only what the walk reads stays live across it; the tile's cell indices, activity and output
+    // pointer are located again afterwards.
+    float best[VPL], px, py, pz[VPL], tcx, tcy, tcz;
+    const Node *nodes;
+    const DistTri *tris;
+    int bvh_nodes, bvh_tris, root;
+    {
+      Cells c0;
+      c0.locate(B, tile, lane);
+#pragma unroll
+      for (int v = 0; v < VPL; ++v) {
+        best[v] = c0.active[v] ? kInf : -1.0f;
+        pz[v] = c0.pz[v];
+      }
+      px = c0.px;
+      py = c0.py;
+      tcx = c0.cx;
+      tcy = c0.cy;
+      tcz = c0.cz;
+      nodes = c0.M->nodes;
+      tris = c0.M->tris;
+      bvh_nodes = c0.M->bvh_nodes;
+      bvh_tris = c0.M->bvh_tris;
+      root = c0.M->root;
+    }
+    const WalkLimits lim = walk_limits<STACK>(bvh_nodes, a.fault);
+    bool done = walk<VPL, STACK, COUNT>(nodes, tris, bvh_nodes, bvh_tris, root, tail, lim, lane, tcx, tcy, tcz, px, py,
+                                        pz, best, ws);
     Cells c;
     c.locate(B, tile, lane);
     const MeshRec &M = *c.M;
-    float best[VPL];
-#pragma unroll
-    for (int v = 0; v < VPL; ++v) best[v] = c.active[v] ? kInf : -1.0f;
-    const WalkLimits lim = walk_limits<STACK>(M.bvh_nodes, a.fault);
-    bool done = walk<VPL, STACK, COUNT>(M.nodes, M.tris, M.bvh_nodes, M.bvh_tris, M.root, tail, lim, lane, c.cx,
-                                        c.cy, c.cz, c.px, c.py, c.pz, best, ws);
     if (!done) {
       unsigned long long slot = 0;
       if (lane == 0) slot = atomicAdd(a.defer_counters, 1ull);
@@ -583,6 +612,13 @@ cudaError_t launch_any(const DistanceArgs &a, int id, int num_sms, cudaStream_t 
 }  // namespace
 
 int tile_shape_count() { return kNumShapes; }
+
+double distance_work_flops(int tile_id, const unsigned long long *w) {
+  int tx, ty, tz;
+  tile_shape(tile_id, tx, ty, tz);
+  const int vpl = tz / (kWarp / (tx * ty));
+  return distance_flops(vpl, double(w[0]), double(w[3]), double(w[4]), double(w[1]));
+}
 
 void tile_shape(int id, int &tx, int &ty, int &tz) {
   const Shape s = kShapes[(id < 0 || id >= kNumShapes) ? 0 : id];

@@ -358,3 +358,5 @@ cudaError_t gwn_enqueue(const GwnInput &in, void *temp, int num_sms, cudaStream_
 }
 
 uint64_t *gwn_refine_counter(void *temp) { return reinterpret_cast<uint64_t *>(static_cast<char *>(temp)) + 1; }
+
+uint64_t *gwn_direct_counter(void *temp) { return reinterpret_cast<uint64_t *>(static_cast<char *>(temp)) + 2; }

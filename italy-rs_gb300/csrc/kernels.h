@@ -165,6 +165,8 @@ struct DistanceArgs {
 };
 
 int tile_shape_count();
+// FP32 flops of the counted distance work (counters as in DistanceArgs::work_counters).
+double distance_work_flops(int tile_id, const unsigned long long *counters);
 // tile shape id -> (tx, ty, tz)
 void tile_shape(int id, int &tx, int &ty, int &tz);
 uint64_t tiles_for(const GridDev &g, int tile_id);

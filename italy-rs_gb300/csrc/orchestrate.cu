@@ -585,11 +585,13 @@ sdfb_status finish_batch(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, const Ba
     sv.sat_tests = w[2];
     sv.plane_tests = w[3];
     sv.rect_tests = w[4];
-    sv.flops_distance = double(w[0]) * kFlopsPointBox + double(w[1]) * kFlopsPointTri +
-                        double(w[3]) * kFlopsPointPlane + double(w[4]) * kFlopsPointRect;
+    sv.flops_distance = distance_work_flops(S.tile_id, w);
     if (S.any_cross)
       cudaMemcpy(&sv.crossings, static_cast<uint64_t *>(ws.col_start.p) + S.total_cols, 8, cudaMemcpyDeviceToHost);
-    if (S.any_gwn) cudaMemcpy(&sv.gwn_fp64_cells, gwn_refine_counter(ws.gwn_tmp.p), 8, cudaMemcpyDeviceToHost);
+    if (S.any_gwn) {
+      cudaMemcpy(&sv.gwn_fp64_cells, gwn_refine_counter(ws.gwn_tmp.p), 8, cudaMemcpyDeviceToHost);
+      cudaMemcpy(&sv.gwn_direct_cells, gwn_direct_counter(ws.gwn_tmp.p), 8, cudaMemcpyDeviceToHost);
+    }
     sv.kernel_launches = S.launched;
     sv.graph_replayed = S.graphed ? 1 : 0;
     cudaMemcpy(&sv.tiles_deferred, static_cast<char *>(ws.misc.p) + kMiscDeferOffset, 8, cudaMemcpyDeviceToHost);

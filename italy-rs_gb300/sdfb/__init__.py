@@ -71,7 +71,7 @@ class Stats(C.Structure):
                 ("crossings", C.c_uint64), ("box_tests", C.c_uint64), ("tri_tests", C.c_uint64),
                 ("flops_distance", C.c_double), ("kernel_launches", C.c_uint64), ("gwn_fp64_cells", C.c_uint64),
                 ("graph_replayed", C.c_uint64), ("tiles_deferred", C.c_uint64),
-                ("plane_tests", C.c_uint64), ("rect_tests", C.c_uint64), ("reserved", C.c_uint64 * 1)]
+                ("plane_tests", C.c_uint64), ("rect_tests", C.c_uint64), ("gwn_direct_cells", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "struct_size")}
