@@ -62,7 +62,7 @@ struct ResidentBvh {
   const sdfb::DistTri *dtris = nullptr;  // distance hierarchy
   const sdfb::TriRec *tris = nullptr;    // winding-number hierarchy
   const uint32_t *leaf_order = nullptr;
-  const float *node_area = nullptr;
+  const float4 *node_moment = nullptr;
   int num_nodes = 0, num_inner = 0, num_tris = 0, root = 0;
 };
 

@@ -7,16 +7,23 @@
 // and its winding number W(q) is an integer, namely the signed count of +z crossings above q
 // (parity.cu stores each crossing's orientation). Then
 //     w(q) = W(q) - w_caps(q),
-// and only the caps -- small triangles hugging the holes -- need solid angles. A cap subtree
-// whose box is at distance d from q subtends at most (area / d^2), so far caps are bounded rather
-// than summed, and a cell is decided as soon as the bound cannot move |w| across 0.5.
+// and only the caps -- small triangles hugging the holes -- need solid angles. A cap subtree far
+// from q is replaced by its dipole term with a rigorous error bound (the far field of Barill et al.
+// 2018, "Fast Winding Numbers for Soups and Clouds", with a Taylor bound of our own): a triangle
+// of area a and unit normal n subtends the integral over it of f(x) = (x - q) . n / |x - q|^3,
+// whose gradient is at most 2 / |x - q|^3 in length. For a cluster inside the ball of radius rho
+// about c, at r = |c - q| > rho,
+//     Omega = D . (c - q) / r^3  +/-  A * 2 rho / (r - rho)^3,    D = sum a_i n_i,  A = sum a_i,
+// with (D, A) stored per node (lbvh.cu) and (c, rho) the child box's centre and half diagonal. A
+// subtree is taken as its dipole when that bound is at most tau, and a cell is decided as soon as
+// the summed bounds cannot move |w| across 0.5.
 //
 // Precision split:
 //   pass 1 (FP32, every cell of every winding-number mesh, warp tiles of 4 x 4 x 2): cells
 //     outside the band (|d| > band_voxels * voxel) whose interval [c - e, c + e] lies on one side
 //     of |w| = 0.5 get their sign; the band and undecided cells go to a refine list.
-//   pass 2 (FP64 accumulation and arithmetic, exact caps from the original FP32 vertices, far
-//     bound threshold 1e-9 sr): signs of the refine list; a cell still undecided goes to
+//   pass 2 (FP64 accumulation and arithmetic, exact caps from the original FP32 vertices, the same
+//     far-field bound per subtree): signs of the refine list; a cell still undecided goes to
 //   pass 3 (FP64 sum over every cap triangle of its mesh, one block per cell).
 #include <algorithm>
 #include <cstdint>
@@ -31,8 +38,11 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kStack = 64;
 constexpr double kInv4Pi = 0.07957747154594767;
-constexpr float kTau32 = 4e-3f;   // sr: expand cap subtrees that may subtend more
-constexpr double kTau64 = 1e-9;
+// Largest far-field error bound (sr) taken for one cap subtree. A cell is decided once the summed
+// bounds cannot move |w| across 0.5; cells far from holes have a margin near 0.5, so the FP64 band
+// pass uses the same bound and only cells it cannot decide go to the direct sum.
+constexpr float kTau32 = 4e-3f;
+constexpr double kTau64 = 4e-3;
 
 template <typename T> struct V3 {
   T x, y, z;
@@ -75,22 +85,51 @@ __device__ __forceinline__ int column_winding(const GwnArgs &a, const MeshRec &M
   return w;
 }
 
-__device__ __forceinline__ float box_d2(float px, float py, float pz, const float4 &n0, const float4 &n1,
-                                        const float4 &n2, int which) {
-  if (which == 0) return box_dist2(px, py, pz, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
-  return box_dist2(px, py, pz, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
+// The far field of a cap cluster -- moment m = (D, A), inside the child box of centre c and half
+// extent e (so inside the ball of radius |e| about c) -- seen from q: false when q is too close
+// (r <= 2 |e|) or the error bound exceeds tau; else val = D . (c - q) / r^3 and err bounds
+// |Omega - val|, widened for the rounding of T.
+template <typename T>
+__device__ __forceinline__ bool far_field(T qx, T qy, T qz, const float4 &n0, const float4 &n1, const float4 &n2,
+                                          int which, const float4 &m, T tau, T &val, T &err) {
+  const float cx = which ? n1.z : n0.x, cy = which ? n1.w : n0.y, cz = which ? n2.x : n0.z;
+  const float ex = which ? n2.y : n0.w, ey = which ? n2.z : n1.x, ez = which ? n2.w : n1.y;
+  const T dx = T(cx) - qx, dy = T(cy) - qy, dz = T(cz) - qz;
+  const T r2 = dx * dx + dy * dy + dz * dz;
+  const T rho = sqrt(T(ex) * T(ex) + T(ey) * T(ey) + T(ez) * T(ez));
+  if (!(r2 > T(4) * rho * rho)) return false;
+  const T r = sqrt(r2), g = r - rho;
+  err = T(m.w) * T(2) * rho / (g * g * g);
+  if (!(err <= tau)) return false;
+  val = (T(m.x) * dx + T(m.y) * dy + T(m.z) * dz) / (r2 * r);
+  constexpr T kRel = sizeof(T) == 4 ? T(1e-5) : T(1e-13);
+  err = err * (T(1) + kRel) + kRel * fabs(val);
+  return true;
 }
 
-// Caps of one mesh seen from q, warp-uniform walk: exact solid angles where some lane needs them,
-// bounds (area / d^2) elsewhere. T is the arithmetic type; exact FP64 leaves read the original
-// cap vertices.
+// (D, A) of a leaf's cap triangles (D = half the sum of their edge cross products).
+__device__ __forceinline__ float4 leaf_moment(const TriRec *tr, int count) {
+  float4 m = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  for (int j = 0; j < count; ++j) {
+    const float4 r3 = __ldg(&tr[j].r3);
+    m.x += 0.5f * r3.x;
+    m.y += 0.5f * r3.y;
+    m.z += 0.5f * r3.z;
+    m.w += 0.5f * sqrtf(r3.x * r3.x + r3.y * r3.y + r3.z * r3.z);
+  }
+  return m;
+}
+
+// Caps of one mesh seen from q, warp-uniform walk: a subtree every lane can take as its far field
+// (error bound <= tau) adds its dipole term to wex and its bound to eps; otherwise the warp
+// descends, and leaves give exact solid angles. T is the arithmetic type; exact FP64 leaves read
+// the original cap vertices.
 template <typename T, bool EXACT64>
-__device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, T qx, T qy, T qz, float tau, T &wex,
+__device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, T qx, T qy, T qz, T tau, T &wex,
                           T &eps, bool &corrupt) {
   const int lane = threadIdx.x & 31;
   int cur = M.cap_root, sp = 0, stk0 = 0, stk1 = 0;
   const long long step_limit = 2ll * M.cap_nodes_n + 64;
-  const float fx = float(qx), fy = float(qy), fz = float(qz);
   auto push = [&](int e) {
     if (sp < kStack) {
       if (sp < 32) {
@@ -121,29 +160,28 @@ __device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, T qx,
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
       if (cnts[k] < 0) continue;
-      const float d2 = box_d2(fx, fy, fz, n0, n1, n2, k);
-      float area;
+      float4 mom;
       if (cnts[k] == 0) {
         if (refs[k] >= M.cap_inner_n) {
           corrupt = true;
           continue;
         }
-        area = __ldg(M.cap_area + refs[k]);
+        mom = __ldg(M.cap_moment + refs[k]);
       } else {
         if (refs[k] < 0 || cnts[k] > M.cap_recs_n - refs[k]) {
           corrupt = true;
           continue;
         }
-        area = 0.0f;
-        for (int j = 0; j < cnts[k]; ++j) {
-          const float4 r3 = __ldg(&M.cap_trec[refs[k] + j].r3);
-          area += 0.5f * sqrtf(r3.x * r3.x + r3.y * r3.y + r3.z * r3.z);
-        }
+        mom = leaf_moment(M.cap_trec + refs[k], cnts[k]);
       }
-      const float bound = d2 > 0.0f ? area / d2 : __int_as_float(0x7f800000);
-      const bool need = active && !(bound <= tau);
+      T val = T(0), err = T(0);
+      const bool far = far_field<T>(qx, qy, qz, n0, n1, n2, k, mom, tau, val, err);
+      const bool need = active && !far;
       if (!__any_sync(kFull, need)) {
-        if (active) eps += T(bound);
+        if (active) {
+          wex += val;
+          eps += err;
+        }
         continue;
       }
       if (cnts[k] == 0) {
@@ -252,7 +290,7 @@ __global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a) {
     const int first_mesh = __shfl_sync(kFull, mesh, 0);
     const bool uniform = __all_sync(kFull, mesh == first_mesh);
     if (uniform) {
-      if (M.cap_root >= 0) caps_walk<double, true>(a, M, active, qx, qy, qz, float(kTau64), wex, eps, corrupt);
+      if (M.cap_root >= 0) caps_walk<double, true>(a, M, active, qx, qy, qz, kTau64, wex, eps, corrupt);
     } else {
       unsigned pending = __ballot_sync(kFull, true);
       while (pending) {
@@ -261,7 +299,7 @@ __global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a) {
         const bool mine = mesh == mm;
         const MeshRec &MM = B.recs[mm];
         if (MM.cap_root >= 0)
-          caps_walk<double, true>(a, MM, active && mine, qx, qy, qz, float(kTau64), wex, eps, corrupt);
+          caps_walk<double, true>(a, MM, active && mine, qx, qy, qz, kTau64, wex, eps, corrupt);
         pending &= ~__ballot_sync(kFull, mine);
       }
     }

@@ -78,7 +78,7 @@ struct MeshRec {
   int cap_nodes_n, cap_inner_n, cap_recs_n;
   const Node *cap_nodes;
   const TriRec *cap_trec;
-  const float *cap_area;
+  const float4 *cap_moment;  // per inner cap node: (area-weighted normal sum, total area)
   const uint32_t *cap_order;
 };
 
@@ -115,7 +115,8 @@ struct BvhDev {
   Node *nodes = nullptr;           // (T_total - 1) inner nodes + M virtual roots
   uint32_t *leaf_order = nullptr;  // local (per-mesh) triangle index of each record
   uint32_t *bounds = nullptr;      // 6 ordered-uint words per mesh: centroid min xyz, max xyz
-  float *node_area = nullptr;      // winding-number hierarchy: total triangle area per inner node
+  float4 *node_moment = nullptr;   // winding-number hierarchy, per inner node: (sum of area x unit
+                                   // normal over its triangles, their total area)
   int num_inner = 0;               // max(T_total - 1, 0)
   int num_nodes = 0;               // num_inner + M
 };

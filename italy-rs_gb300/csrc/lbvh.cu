@@ -17,7 +17,8 @@
 //                  mesh starts there.
 //   8. k_gather    triangle records in leaf order: 80-byte frame records (DistTri) for the
 //                  distance hierarchy, the k_prep records for the winding-number hierarchy.
-//   9. k_areas     (optional) total triangle area per inner node.
+//   9. k_moments   (optional) per inner node the sum of area x unit normal of its triangles and
+//                  their total area (the winding number's far field, gwn.cu).
 #include <algorithm>
 #include <cstdint>
 
@@ -408,15 +409,17 @@ __global__ __launch_bounds__(kThreads) void k_gather(BatchDev B, const uint32_t 
   order[k] = static_cast<uint32_t>(lt);
 }
 
-// Total triangle area of every inner node, bottom-up like k_refit (bounds the solid angle a
-// subtree can subtend: at distance d from its box it is at most area / d^2).
-__device__ __forceinline__ float tri_area(const TriRec &t) {
-  return 0.5f * sqrtf(t.r3.x * t.r3.x + t.r3.y * t.r3.y + t.r3.z * t.r3.z);
+// Far-field moments of every inner node, bottom-up like k_refit: (sum of a_i n_i, sum of a_i)
+// over its triangles, a_i the area and n_i the unit normal. A triangle's a_i n_i is half its edge
+// cross product, the r3 of its record.
+__device__ __forceinline__ float4 tri_moment(const TriRec &t) {
+  return make_float4(0.5f * t.r3.x, 0.5f * t.r3.y, 0.5f * t.r3.z,
+                     0.5f * sqrtf(t.r3.x * t.r3.x + t.r3.y * t.r3.y + t.r3.z * t.r3.z));
 }
 
-__global__ __launch_bounds__(kThreads) void k_areas(int n, const TriRec *__restrict__ tris,
-                                                    const int2 *__restrict__ child, const int *__restrict__ iparent,
-                                                    const int *__restrict__ lparent, int *visits, float *area) {
+__global__ __launch_bounds__(kThreads) void k_moments(int n, const TriRec *__restrict__ tris,
+                                                      const int2 *__restrict__ child, const int *__restrict__ iparent,
+                                                      const int *__restrict__ lparent, int *visits, float4 *mom) {
   const int leaf = blockIdx.x * kThreads + threadIdx.x;
   if (leaf >= n) return;
   int node = lparent[leaf];
@@ -425,9 +428,9 @@ __global__ __launch_bounds__(kThreads) void k_areas(int n, const TriRec *__restr
     if (atomicAdd(visits + node, 1) == 0) return;
     __threadfence();
     const int2 c = child[node];
-    const float a = c.x < 0 ? tri_area(tris[c.x & 0x7fffffff]) : __ldcg(area + c.x);
-    const float b = c.y < 0 ? tri_area(tris[c.y & 0x7fffffff]) : __ldcg(area + c.y);
-    __stcg(area + node, a + b);
+    const float4 a = c.x < 0 ? tri_moment(tris[c.x & 0x7fffffff]) : __ldcg(mom + c.x);
+    const float4 b = c.y < 0 ? tri_moment(tris[c.y & 0x7fffffff]) : __ldcg(mom + c.y);
+    __stcg(mom + node, make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w));
     node = iparent[node];
   }
 }
@@ -441,7 +444,7 @@ size_t lbvh_temp_bytes(uint64_t total_tris, int num_meshes) { return temp_layout
 size_t lbvh_bytes(uint64_t T, int M, bool winding) {
   const size_t n = std::max<uint64_t>(T, 1), m = std::max<uint64_t>(T, 2) - 1;
   return align256(n * (winding ? sizeof(TriRec) : sizeof(DistTri))) + align256((m + M) * sizeof(Node)) +
-         align256(n * 4) + align256(size_t(M) * 6 * 4) + (winding ? align256(m * sizeof(float)) : 0);
+         align256(n * 4) + align256(size_t(M) * 6 * 4) + (winding ? align256(m * sizeof(float4)) : 0);
 }
 
 void lbvh_bind(BvhDev &b, void *mem, uint64_t T, int M, bool winding) {
@@ -456,7 +459,7 @@ void lbvh_bind(BvhDev &b, void *mem, uint64_t T, int M, bool winding) {
   p += align256(n * 4);
   b.bounds = reinterpret_cast<uint32_t *>(p);
   p += align256(size_t(M) * 6 * 4);
-  b.node_area = winding ? reinterpret_cast<float *>(p) : nullptr;
+  b.node_moment = winding ? reinterpret_cast<float4 *>(p) : nullptr;
   b.num_inner = T >= 2 ? static_cast<int>(T - 1) : 0;
   b.num_nodes = b.num_inner + M;
 }
@@ -507,9 +510,9 @@ cudaError_t lbvh_build(const BatchDev &B, BvhDev &b, void *temp, size_t temp_byt
   note_launch();
   k_gather<<<blocks_for(T), kThreads, 0, st>>>(B, vals, t.rec, b.tris, b.dtris, b.leaf_order);
   note_launch();
-  if (b.node_area && T >= 2) {
+  if (b.node_moment && T >= 2) {
     if ((e = cudaMemsetAsync(t.visits, 0, sizeof(int) * (T - 1), st)) != cudaSuccess) return e;
-    k_areas<<<blocks_for(T), kThreads, 0, st>>>(n, b.tris, t.child, t.iparent, t.lparent, t.visits, b.node_area);
+    k_moments<<<blocks_for(T), kThreads, 0, st>>>(n, b.tris, t.child, t.iparent, t.lparent, t.visits, b.node_moment);
     note_launch();
   }
   return cudaGetLastError();

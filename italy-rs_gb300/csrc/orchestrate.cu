@@ -239,7 +239,7 @@ void make_layout(sdfb_ctx *ctx, const std::vector<PlanMesh> &ms, const sdfb_opts
         r.cap_root = p.caps->root;
         r.cap_nodes = p.caps->nodes;
         r.cap_trec = p.caps->tris;
-        r.cap_area = p.caps->node_area;
+        r.cap_moment = p.caps->node_moment;
         r.cap_order = p.caps->leaf_order;
         r.cap_nodes_n = p.caps->num_nodes;
         r.cap_inner_n = p.caps->num_inner;
@@ -297,7 +297,7 @@ void bind_built(Layout &L, const BvhDev &bvh, const BvhDev *caps) {
     if (caps && r.cap_root >= 0 && !r.cap_nodes) {
       r.cap_nodes = caps->nodes;
       r.cap_trec = caps->tris;
-      r.cap_area = caps->node_area;
+      r.cap_moment = caps->node_moment;
       r.cap_order = caps->leaf_order;
       r.cap_nodes_n = caps->num_nodes;
       r.cap_inner_n = caps->num_inner;
@@ -672,7 +672,7 @@ sdfb_status build_resident(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, const 
     o.dtris = b.dtris;
     o.tris = b.tris;
     o.leaf_order = b.leaf_order;
-    o.node_area = b.node_area;
+    o.node_moment = b.node_moment;
     o.num_nodes = b.num_nodes;
     o.num_inner = b.num_inner;
     o.num_tris = static_cast<int>(T);
