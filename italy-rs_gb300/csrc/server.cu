@@ -48,21 +48,39 @@ double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-// Content hash of a mesh (FNV-1a over 8-byte words, then a final avalanche).
-uint64_t content_hash(const void *p, size_t n, uint64_t h) {
-  const uint8_t *b = static_cast<const uint8_t *>(p);
-  size_t i = 0;
-  for (; i + 8 <= n; i += 8) {
-    uint64_t w;
-    std::memcpy(&w, b + i, 8);
-    h = (h ^ w) * 0x100000001b3ull;
-    h ^= h >> 29;
-  }
-  for (; i < n; ++i) h = (h ^ b[i]) * 0x100000001b3ull;
+// Two independent 64-bit content hashes of a byte range, in one pass over 8-byte words: h.a
+// multiplies by the FNV prime and folds high bits down, h.b adds each word to a golden-ratio
+// multiply-rotate chain; both end in an avalanche. A mesh's id is its a-hash; the b-hash and the
+// vertex and triangle counts are compared on every cache hit, so two meshes whose ids collide are
+// never taken for each other.
+struct Hash2 {
+  uint64_t a = 0xcbf29ce484222325ull, b = 0x6a09e667f3bcc909ull;
+};
+
+inline uint64_t avalanche(uint64_t h) {
   h ^= h >> 33;
   h *= 0xff51afd7ed558ccdull;
   h ^= h >> 33;
+  h *= 0xc4ceb9fe1a85ec53ull;
+  h ^= h >> 33;
   return h;
+}
+
+void content_hash(const void *p, size_t n, Hash2 &h) {
+  const uint8_t *bytes = static_cast<const uint8_t *>(p);
+  size_t i = 0;
+  for (; i + 8 <= n; i += 8) {
+    uint64_t w;
+    std::memcpy(&w, bytes + i, 8);
+    h.a = (h.a ^ w) * 0x100000001b3ull;
+    h.a ^= h.a >> 29;
+    h.b = (h.b + w) * 0x9e3779b97f4a7c15ull;
+    h.b = (h.b << 31) | (h.b >> 33);
+  }
+  for (; i < n; ++i) {
+    h.a = (h.a ^ bytes[i]) * 0x100000001b3ull;
+    h.b = (h.b + bytes[i]) * 0x9e3779b97f4a7c15ull;
+  }
 }
 
 // Stream-ordered device allocation (no device-wide synchronisation when freed).
@@ -73,6 +91,7 @@ struct AsyncBuf {
 
 struct Resident {
   uint64_t id = 0;
+  uint64_t check = 0;  // the second content hash, compared with V and T on a cache hit
   AsyncBuf verts, idx, pverts, pidx, cidx, bvh, caps;
   ResidentBvh tree, cap_tree;
   uint32_t V = 0, T = 0, pV = 0, pT = 0, cT = 0;
@@ -511,21 +530,32 @@ sdfb_status sdfb_mesh_register(sdfb_server *srv, const float *verts, uint32_t nu
   if (num_tris == 0 || num_verts == 0) return srv->fail(SDFB_ERR_BAD_MESH, "mesh has no triangles");
   for (size_t k = 0; k < size_t(num_tris) * 3; ++k)
     if (idx[k] >= num_verts) return srv->fail(SDFB_ERR_BAD_MESH, "triangle index out of range");
-  uint64_t h = content_hash(verts, size_t(num_verts) * 12, 0xcbf29ce484222325ull);
-  h = content_hash(idx, size_t(num_tris) * 12, h);
-  h = content_hash(&num_verts, 4, h);
-  *mesh_id = h;
-  // A cache hit returns at once. Otherwise this thread takes a free registration slot and builds
-  // the mesh, unless another thread is already building the same mesh: then it waits for that
-  // build (a second build would replace a Resident that queued requests may point to).
+  Hash2 hh;
+  const uint32_t counts[2] = {num_verts, num_tris};
+  content_hash(counts, sizeof counts, hh);
+  content_hash(verts, size_t(num_verts) * 12, hh);
+  content_hash(idx, size_t(num_tris) * 12, hh);
+  uint64_t h = avalanche(hh.a);
+  const uint64_t check = avalanche(hh.b);
+  // A cache hit (same id, second hash and counts) returns at once. An id held by other contents
+  // moves this mesh on to the next id in a fixed probe sequence. Otherwise this thread takes a free
+  // registration slot and builds the mesh, unless another thread is already building under the
+  // same id: then it waits for that build and looks again (a second build would replace a
+  // Resident that queued requests may point to).
   int slot = -1;
   {
     std::unique_lock<std::mutex> lk(srv->mu);
     for (;;) {
       auto it = srv->meshes.find(h);
       if (it != srv->meshes.end()) {
-        it->second->last_use = ++srv->tick;
-        return SDFB_OK;
+        const Resident &m = *it->second;
+        if (m.check == check && m.V == num_verts && m.T == num_tris) {
+          it->second->last_use = ++srv->tick;
+          *mesh_id = h;
+          return SDFB_OK;
+        }
+        h = avalanche(h + 0x9e3779b97f4a7c15ull);  // another mesh holds this id
+        continue;
       }
       if (!srv->building.count(h)) {
         for (size_t k = 0; k < srv->reg_busy.size(); ++k)
@@ -557,6 +587,8 @@ sdfb_status sdfb_mesh_register(sdfb_server *srv, const float *verts, uint32_t nu
   cudaSetDevice(srv->device);
   auto r = std::make_unique<Resident>();
   r->id = h;
+  r->check = check;
+  *mesh_id = h;
   r->V = num_verts;
   r->T = num_tris;
   const size_t bvh_bytes = resident_bytes(num_tris, false);
