@@ -23,7 +23,7 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["primitives.cu", "lbvh.cu", "occupancy.cu", "parity.cu", "distance.cu", "sparse.cu", "gwn.cu",
               "orchestrate.cu", "server.cu", "noalloc.cu", "materials.cu",
-              "consumer.cu", "weld.cu", "api.cu"]
+              "consumer.cu", "weld.cu", "caps.cu", "api.cu"]
 CPP_SOURCES = ["host_mesh.cpp"]
 
 

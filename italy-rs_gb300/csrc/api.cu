@@ -76,7 +76,8 @@ sdfb_ctx::~sdfb_ctx() {
 DevBuf *sdfb_ctx::all_bufs(int i) {
   DevBuf *b[] = {&in_verts, &in_idx,   &in_verts2, &in_idx2,    &in_caps,   &in_capidx, &out_dist,
                  &out_occ,  &first_tri, &sparse_tmp, &sparse_out, &mat_rec,  &mat_in,    &mat_tri,
-                 &hit_keys, &hit_vals,  &hit_alt,   &mat_cells, &cons_grid, &cons_io,    &weld_tmp};
+                 &hit_keys, &hit_vals,  &hit_alt,   &mat_cells, &cons_grid, &cons_io,    &weld_tmp,
+                 &caps_tmp, &caps_misc};
   return i < int(sizeof b / sizeof b[0]) ? b[i] : nullptr;
 }
 
@@ -165,43 +166,6 @@ int resolve_sign(const sdfb_opts &o, const float *hv, uint32_t V, const uint32_t
   return w == 1 ? kSignParity : kSignGwn;
 }
 
-sdfb_status upload_caps(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &ms, std::vector<CapBuild> &caps) {
-  size_t nv = 0, np = 0, nc = 0;
-  for (size_t m = 0; m < ms.size(); ++m)
-    if (ms[m].sign == kSignGwn) {
-      nv += caps[m].verts.size();
-      np += caps[m].pidx.size();
-      nc += caps[m].cidx.size();
-    }
-  if (nv == 0) return SDFB_OK;
-  ENSURE(ctx->in_caps, nv * 4);
-  ENSURE(ctx->in_idx2, np * 4);
-  ENSURE(ctx->in_capidx, std::max<size_t>(nc, 1) * 4);
-  size_t ov = 0, op = 0, oc = 0;
-  for (size_t m = 0; m < ms.size(); ++m) {
-    if (ms[m].sign != kSignGwn) continue;
-    const CapBuild &c = caps[m];
-    float *dv = static_cast<float *>(ctx->in_caps.p) + ov;
-    uint32_t *dp = static_cast<uint32_t *>(ctx->in_idx2.p) + op;
-    uint32_t *dc = static_cast<uint32_t *>(ctx->in_capidx.p) + oc;
-    CK(cudaMemcpyAsync(dv, c.verts.data(), c.verts.size() * 4, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(dp, c.pidx.data(), c.pidx.size() * 4, cudaMemcpyHostToDevice, st));
-    if (!c.cidx.empty()) CK(cudaMemcpyAsync(dc, c.cidx.data(), c.cidx.size() * 4, cudaMemcpyHostToDevice, st));
-    ms[m].pverts = dv;
-    ms[m].pidx = dp;
-    ms[m].pV = static_cast<uint32_t>(c.verts.size() / 3);
-    ms[m].pT = static_cast<uint32_t>(c.pidx.size() / 3);
-    ms[m].cverts = dv;
-    ms[m].cidx = dc;
-    ms[m].cT = static_cast<uint32_t>(c.cidx.size() / 3);
-    ov += c.verts.size();
-    op += c.pidx.size();
-    oc += c.cidx.size();
-  }
-  // the caps arrays are host vectors read by asynchronous copies: wait before they go away
-  CK(cudaStreamSynchronize(st));
-  return SDFB_OK;
-}
 
 // The device address of a page-locked host buffer (cudaHostAlloc, cudaHostRegister, a pinned
 // tensor), or null for pageable memory. The distance kernel writes such a distance output
@@ -220,6 +184,66 @@ void *mapped_host(void *p) {
 }
 
 }  // namespace
+
+sdfb_status device_caps(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &ms, bool every_gwn) {
+  // Regions sized for the most caps a mesh can have (3T boundary half-edges, 3T loops).
+  size_t nv = 0, np = 0, tmax = 0, ng = 0;
+  for (const PlanMesh &p : ms)
+    if (p.sign == kSignGwn && (p.dist || every_gwn)) {
+      const size_t V = p.pverts ? p.pV : p.V, T = p.pverts ? p.pT : p.T;
+      nv += 3 * (V + 3 * T);
+      np += 3 * (T + 3 * T);
+      tmax = std::max<size_t>(tmax, T);
+      ++ng;
+    }
+  if (ng == 0) return SDFB_OK;
+  ENSURE(ctx->in_caps, nv * 4);
+  ENSURE(ctx->in_capidx, np * 4);
+  ENSURE(ctx->caps_tmp, caps_temp_bytes(tmax));
+  ENSURE(ctx->caps_misc, 256 + ng * 16);
+  uint32_t *d_err = static_cast<uint32_t *>(ctx->caps_misc.p);
+  uint64_t *d_tot = reinterpret_cast<uint64_t *>(static_cast<char *>(ctx->caps_misc.p) + 256);
+  CK(cudaMemsetAsync(d_err, 0, 4, st));
+  size_t ov = 0, op = 0, k = 0;
+  std::vector<size_t> at(ms.size(), 0);
+  for (size_t m = 0; m < ms.size(); ++m) {
+    PlanMesh &p = ms[m];
+    if (p.sign != kSignGwn || !(p.dist || every_gwn)) continue;
+    const float *bv = p.pverts ? p.pverts : p.verts;
+    const uint32_t *bi = p.pverts ? p.pidx : p.idx;
+    const uint32_t V = p.pverts ? p.pV : p.V, T = p.pverts ? p.pT : p.T;
+    float *dv = static_cast<float *>(ctx->in_caps.p) + ov;
+    uint32_t *dp = static_cast<uint32_t *>(ctx->in_capidx.p) + op;
+    CK(cudaMemcpyAsync(dv, bv, size_t(V) * 12, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(dp, bi, size_t(T) * 12, cudaMemcpyDeviceToDevice, st));
+    CK(caps_device(bv, V, bi, T, ctx->caps_tmp.p, ctx->caps_tmp.cap, dv + 3 * size_t(V), dp + 3 * size_t(T),
+                   d_tot + 2 * k, d_err, ctx->num_sms, st));
+    p.pverts = p.cverts = dv;
+    p.pidx = dp;
+    p.cidx = dp + 3 * size_t(T);
+    p.pV = V;
+    p.pT = T;
+    at[m] = k++;
+    ov += 3 * (size_t(V) + 3 * size_t(T));
+    op += 3 * (size_t(T) + 3 * size_t(T));
+  }
+  std::vector<uint64_t> tot(2 * ng);
+  uint32_t h_err = 0;
+  CK(cudaMemcpyAsync(tot.data(), d_tot, tot.size() * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&h_err, d_err, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (h_err & kErrBadIndex) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "triangle index out of range");
+  if (h_err) return ctx_fail(ctx, SDFB_ERR_INTERNAL, "boundary loops of a winding-number mesh do not close");
+  for (size_t m = 0; m < ms.size(); ++m) {
+    PlanMesh &p = ms[m];
+    if (p.sign != kSignGwn || !(p.dist || every_gwn)) continue;
+    const uint64_t caps = tot[2 * at[m]], loops = tot[2 * at[m] + 1];
+    p.pV += static_cast<uint32_t>(loops);
+    p.pT += static_cast<uint32_t>(caps);
+    p.cT = static_cast<uint32_t>(caps);
+  }
+  return SDFB_OK;
+}
 
 sdfb_status device_sign(sdfb_ctx *ctx, const sdfb_opts &o, const float *d_verts, uint32_t V, const uint32_t *d_idx,
                         uint32_t T, cudaStream_t st, int *sign, int *watertight) {
@@ -340,21 +364,9 @@ sdfb_status sdfb_bake_device(sdfb_ctx *ctx, const float *d_verts, uint32_t num_v
   p.grid = *grid;
   p.dist = o.no_distance ? nullptr : d_dist_out;
   p.occ = o.no_occupancy ? nullptr : d_occ_out;
-  std::vector<CapBuild> caps(1);
   sdfb_status s = device_sign(ctx, o, d_verts, num_verts, d_idx, num_tris, st, &p.sign, &p.watertight);
   if (s != SDFB_OK) return s;
-  if (p.sign == kSignGwn && p.dist) {
-    // the caps are built on the host
-    std::vector<float> hv(size_t(num_verts) * 3);
-    std::vector<uint32_t> hi(size_t(num_tris) * 3);
-    CK(cudaMemcpyAsync(hv.data(), d_verts, hv.size() * 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(hi.data(), d_idx, hi.size() * 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    for (size_t k = 0; k < hi.size(); ++k)
-      if (hi[k] >= num_verts) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "triangle index out of range");
-    build_caps(hv.data(), num_verts, hi.data(), num_tris, caps[0]);
-    if ((s = upload_caps(ctx, st, ms, caps)) != SDFB_OK) return s;
-  }
+  if ((s = device_caps(ctx, st, ms)) != SDFB_OK) return s;
   return run_batch(ctx, st, ms, o, false, stats);
 }
 
@@ -382,12 +394,6 @@ sdfb_status sdfb_bake(sdfb_ctx *ctx, const float *verts, uint32_t num_verts, con
   sdfb_status sg = device_sign(ctx, o, static_cast<const float *>(ctx->in_verts.p), num_verts,
                                static_cast<const uint32_t *>(ctx->in_idx.p), num_tris, st, &p.sign, &p.watertight);
   if (sg != SDFB_OK) return sg;
-  std::vector<CapBuild> caps(1);
-  if (p.sign == kSignGwn && want_dist) {
-    for (size_t k = 0; k < size_t(num_tris) * 3; ++k)
-      if (idx[k] >= num_verts) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "triangle index out of range");
-    build_caps(verts, num_verts, idx, num_tris, caps[0]);
-  }
   p.verts = static_cast<const float *>(ctx->in_verts.p);
   p.idx = static_cast<const uint32_t *>(ctx->in_idx.p);
   p.V = num_verts;
@@ -398,11 +404,9 @@ sdfb_status sdfb_bake(sdfb_ctx *ctx, const float *verts, uint32_t num_verts, con
   uint8_t *const direct_occ = nullptr;
   p.dist = want_dist ? (direct_dist ? direct_dist : static_cast<float *>(ctx->out_dist.p)) : nullptr;
   p.occ = want_occ ? (direct_occ ? direct_occ : static_cast<uint8_t *>(ctx->out_occ.p)) : nullptr;
-  if (p.sign == kSignGwn && want_dist) {
-    const sdfb_status s = upload_caps(ctx, st, ms, caps);
-    if (s != SDFB_OK) return s;
-  }
-  const sdfb_status s = run_batch(ctx, st, ms, o, false, stats);
+  sdfb_status s = device_caps(ctx, st, ms);
+  if (s != SDFB_OK) return s;
+  s = run_batch(ctx, st, ms, o, false, stats);
   if (s != SDFB_OK) return s;
   if (want_dist && !direct_dist)
     CK(cudaMemcpyAsync(dist_out, ctx->out_dist.p, cells * 4, cudaMemcpyDeviceToHost, st));
@@ -469,15 +473,12 @@ sdfb_status sdfb_bake_soup(sdfb_ctx *ctx, const float *positions, uint32_t num_t
   p.dist = want_dist ? (direct_dist ? direct_dist : static_cast<float *>(ctx->out_dist.p)) : nullptr;
   p.occ = want_occ ? static_cast<uint8_t *>(ctx->out_occ.p) : nullptr;
   if (p.sign == kSignGwn && want_dist) {
-    // the caps are built on the host from the welded mesh
-    std::vector<uint32_t> welded(V);
-    std::vector<float> uniq(size_t(U) * 3);
-    CK(cudaMemcpyAsync(welded.data(), d_welded, size_t(V) * 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(uniq.data(), ctx->in_verts2.p, size_t(U) * 12, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    std::vector<CapBuild> caps(1);
-    build_caps(uniq.data(), U, welded.data(), num_tris, caps[0]);
-    if ((s = upload_caps(ctx, st, ms, caps)) != SDFB_OK) return s;
+    // the caps close the welded mesh
+    p.pverts = static_cast<const float *>(ctx->in_verts2.p);
+    p.pidx = d_welded;
+    p.pV = U;
+    p.pT = num_tris;
+    if ((s = device_caps(ctx, st, ms)) != SDFB_OK) return s;
   } else if (p.sign == kSignParity && want_dist) {
     p.pverts = static_cast<const float *>(ctx->in_verts2.p);
     p.pidx = static_cast<const uint32_t *>(ctx->in_idx2.p);
@@ -670,8 +671,6 @@ sdfb_status sdfb_bake_batch_device(sdfb_ctx *ctx, uint32_t count, const sdfb_mes
   const sdfb_opts o = opts_or_default(opts);
   cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
   std::vector<PlanMesh> ms(count);
-  std::vector<CapBuild> caps(count);
-  bool any_gwn = false;
   for (uint32_t m = 0; m < count; ++m) {
     const sdfb_mesh_desc &d = meshes[m];
     if (!d.verts || !d.idx || !grid_ok(&grids[m]))
@@ -690,22 +689,9 @@ sdfb_status sdfb_bake_batch_device(sdfb_ctx *ctx, uint32_t count, const sdfb_mes
       const std::string e = ctx->err;
       return ctx_fail(ctx, sg, "mesh %u: %s", m, e.c_str());
     }
-    if (p.sign == kSignGwn && p.dist) {
-      std::vector<float> hv(size_t(d.num_verts) * 3);
-      std::vector<uint32_t> hi(size_t(d.num_tris) * 3);
-      CK(cudaMemcpyAsync(hv.data(), d.verts, hv.size() * 4, cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(hi.data(), d.idx, hi.size() * 4, cudaMemcpyDeviceToHost, st));
-      CK(cudaStreamSynchronize(st));
-      for (size_t k = 0; k < hi.size(); ++k)
-        if (hi[k] >= d.num_verts) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh %u: triangle index out of range", m);
-      build_caps(hv.data(), d.num_verts, hi.data(), d.num_tris, caps[m]);
-      any_gwn = true;
-    }
   }
-  if (any_gwn) {
-    const sdfb_status s = upload_caps(ctx, st, ms, caps);
-    if (s != SDFB_OK) return s;
-  }
+  const sdfb_status s = device_caps(ctx, st, ms);
+  if (s != SDFB_OK) return s;
   return run_batch(ctx, st, ms, o, true, stats);
 }
 
@@ -731,10 +717,8 @@ sdfb_status sdfb_bake_batch(sdfb_ctx *ctx, uint32_t count, const sdfb_mesh_desc 
   ENSURE(ctx->in_verts, nv * 4);
   ENSURE(ctx->in_idx, ni * 4);
   std::vector<PlanMesh> ms(count);
-  std::vector<CapBuild> caps(count);
   std::vector<float *> direct_dist(count, nullptr);
   std::vector<uint8_t *> direct_occ(count, nullptr);
-  bool any_gwn = false;
   size_t ov = 0, oi = 0;
   uint64_t occ_off = 0;
   for (uint32_t m = 0; m < count; ++m) {
@@ -756,12 +740,6 @@ sdfb_status sdfb_bake_batch(sdfb_ctx *ctx, uint32_t count, const sdfb_mesh_desc 
     p.grid = grids[m];
     if (want_dist && dist_outs[m] && p.sign != kSignGwn)
       direct_dist[m] = static_cast<float *>(mapped_host(dist_outs[m]));
-    if (p.sign == kSignGwn && want_dist && dist_outs[m]) {
-      for (size_t k = 0; k < size_t(d.num_tris) * 3; ++k)
-        if (d.idx[k] >= d.num_verts) return ctx_fail(ctx, SDFB_ERR_BAD_MESH, "mesh %u: triangle index out of range", m);
-      build_caps(d.verts, d.num_verts, d.idx, d.num_tris, caps[m]);
-      any_gwn = true;
-    }
     ov += size_t(d.num_verts) * 3;
     oi += size_t(d.num_tris) * 3;
   }
@@ -784,11 +762,9 @@ sdfb_status sdfb_bake_batch(sdfb_ctx *ctx, uint32_t count, const sdfb_mesh_desc 
       p.occ = direct_occ[m] ? direct_occ[m] : static_cast<uint8_t *>(ctx->out_occ.p) + occ_off;
     if (stage) occ_off += cells;
   }
-  if (any_gwn) {
-    const sdfb_status s = upload_caps(ctx, st, ms, caps);
-    if (s != SDFB_OK) return s;
-  }
-  const sdfb_status s = run_batch(ctx, st, ms, o, true, stats);
+  sdfb_status s = device_caps(ctx, st, ms);
+  if (s != SDFB_OK) return s;
+  s = run_batch(ctx, st, ms, o, true, stats);
   if (s != SDFB_OK) return s;
   for (uint32_t m = 0; m < count; ++m) {
     const uint64_t cells = uint64_t(ms[m].grid.nx) * ms[m].grid.ny * ms[m].grid.nz;

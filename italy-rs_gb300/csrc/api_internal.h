@@ -87,15 +87,6 @@ struct PlanMesh {
   const ResidentBvh *caps = nullptr;  // set: the caps hierarchy of a resident winding-number mesh
 };
 
-// Host-side result of capping a mesh for the winding-number sign.
-struct CapBuild {
-  std::vector<float> verts;    // mesh vertices followed by the loop centres
-  std::vector<uint32_t> pidx;  // mesh triangles followed by the cap triangles
-  std::vector<uint32_t> cidx;  // cap triangles alone
-  size_t loops = 0;
-};
-// Builds the crossing mesh (mesh + caps) and the caps of an indexed mesh.
-void build_caps(const float *verts, uint32_t V, const uint32_t *idx, uint32_t T, CapBuild &out);
 
 struct GwnInput {
   sdfb::BatchDev batch;
@@ -150,6 +141,7 @@ struct sdfb_ctx {
   DevBuf mat_rec, mat_in, mat_tri, hit_keys, hit_vals, hit_alt, mat_cells;
   DevBuf cons_grid, cons_io;  // consumer check: a grid and its queries / results
   DevBuf weld_tmp;            // device weld / watertight census
+  DevBuf caps_tmp, caps_misc; // device-built winding-number caps: temporaries, totals and error word
   PinBuf staging_small;
   Workspace ws;
   int tuned_leaf[32][8];  // [log2 T][log2 n - 4]
@@ -203,6 +195,20 @@ sdfb_status run_batch(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &mes
 size_t resident_bytes(uint64_t tris, bool winding = false);
 sdfb_status build_resident(sdfb_ctx *ctx, Workspace &ws, cudaStream_t st, const PlanMesh &mesh, void *mem,
                            ResidentBvh &out, void *cap_mem, ResidentBvh &cap_out);
+
+// caps.cu: boundary caps of an indexed mesh on the device. centres receives up to 3T loop centres
+// (3 floats each), cap_tris up to 3T cap triangles (indices; centre c is vertex V + c); totals[0] =
+// cap triangles (boundary half-edges), totals[1] = loops. Enqueued only.
+size_t caps_temp_bytes(uint64_t T);
+cudaError_t caps_device(const float *verts, uint32_t V, const uint32_t *idx, uint32_t T, void *temp,
+                        size_t temp_bytes, float *centres, uint32_t *cap_tris, uint64_t *totals, uint32_t *err,
+                        int num_sms, cudaStream_t st);
+// The crossing mesh (mesh + caps) and the caps of every winding-number mesh of ms that has a
+// distance output, built on the device into the context's buffers; sets their pverts / pidx /
+// cverts / cidx and counts. The caps close the crossing mesh already set (pverts / pidx, as the
+// soup bake's welded mesh), else the mesh itself. One read of the totals synchronises the stream.
+// every_gwn: also the winding-number meshes without a distance output (resident meshes).
+sdfb_status device_caps(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &ms, bool every_gwn = false);
 
 // gwn.cu: flips the sign of cells whose generalized winding number says inside (enqueued only).
 size_t gwn_temp_bytes(uint64_t gwn_cells);

@@ -2,8 +2,8 @@
 // vote of src/render/kernels/sdf_bake.cu:53-69, which assumes a closed mesh).
 //
 // w(q) = sum of triangle solid angles / 4 pi (Jacobson, Kavan & Sorkine-Hornung 2013); a cell is
-// inside when |w| > 0.5. It is evaluated through an exact decomposition: the host closes every
-// boundary loop of the mesh with a small fan cap (host_mesh.cpp), so mesh + caps has no boundary
+// inside when |w| > 0.5. It is evaluated through an exact decomposition: the bake closes every
+// boundary loop of the mesh with a small fan cap (caps.cu), so mesh + caps has no boundary
 // and its winding number W(q) is an integer, namely the signed count of +z crossings above q
 // (parity.cu stores each crossing's orientation). Then
 //     w(q) = W(q) - w_caps(q),

@@ -120,87 +120,6 @@ int indexed_mesh_watertight(const float *verts, uint32_t V, const uint32_t *idx,
   return watertight_flag(tri.data(), T, &b, &m);
 }
 
-size_t boundary_caps(const float *verts, uint32_t V, const uint32_t *idx, uint32_t T, std::vector<float> &cap_verts,
-                     std::vector<uint32_t> &cap_idx) {
-  cap_verts.clear();
-  cap_idx.clear();
-  // Net directed multiplicity per undirected edge (u < v): +1 for u->v, -1 for v->u.
-  const size_t cap = table_size(3 * size_t(T));
-  std::vector<uint64_t> keys(cap, ~0ull);
-  std::vector<int32_t> net(cap, 0);
-  std::vector<size_t> used_slots;
-  used_slots.reserve(3 * size_t(T));
-  for (size_t t = 0; t < T; ++t) {
-    for (int k = 0; k < 3; ++k) {
-      const uint32_t a = idx[3 * t + k], b = idx[3 * t + (k + 1) % 3];
-      if (a == b) continue;
-      const uint32_t u = a < b ? a : b, v = a < b ? b : a;
-      const uint64_t key = (uint64_t(u) << 32) | v;
-      size_t s = mix64(key) & (cap - 1);
-      while (keys[s] != ~0ull && keys[s] != key) s = (s + 1) & (cap - 1);
-      if (keys[s] == ~0ull) {
-        keys[s] = key;
-        used_slots.push_back(s);
-      }
-      net[s] += (a == u) ? 1 : -1;
-    }
-  }
-  // Boundary half-edges, grouped by tail vertex.
-  std::vector<std::pair<uint32_t, uint32_t>> half;
-  for (size_t s : used_slots) {
-    const int32_t n = net[s];
-    if (n == 0) continue;
-    const uint32_t u = uint32_t(keys[s] >> 32), v = uint32_t(keys[s] & 0xffffffffu);
-    for (int32_t r = 0; r < (n > 0 ? n : -n); ++r) half.push_back(n > 0 ? std::make_pair(u, v) : std::make_pair(v, u));
-  }
-  if (half.empty()) return 0;
-  std::sort(half.begin(), half.end());
-  std::vector<uint8_t> done(half.size(), 0);
-  // first half-edge of each tail vertex (half is sorted by tail)
-  auto first_of = [&](uint32_t tail) {
-    return size_t(std::lower_bound(half.begin(), half.end(), std::make_pair(tail, 0u)) - half.begin());
-  };
-  std::vector<size_t> cursor_cache;
-  size_t loops = 0;
-  std::vector<uint32_t> loop;
-  for (size_t h0 = 0; h0 < half.size(); ++h0) {
-    if (done[h0]) continue;
-    loop.clear();
-    size_t h = h0;
-    const uint32_t start = half[h0].first;
-    // Walk until the chain returns to the start vertex; degrees balance, so it always does.
-    for (size_t guard = 0; guard <= half.size(); ++guard) {
-      done[h] = 1;
-      loop.push_back(half[h].first);
-      const uint32_t head = half[h].second;
-      if (head == start) break;
-      size_t nh = first_of(head);
-      while (nh < half.size() && half[nh].first == head && done[nh]) ++nh;
-      if (nh >= half.size() || half[nh].first != head) break;  // unbalanced input: leave open
-      h = nh;
-    }
-    double cx = 0, cy = 0, cz = 0;
-    for (uint32_t w : loop) {
-      cx += verts[3 * size_t(w)];
-      cy += verts[3 * size_t(w) + 1];
-      cz += verts[3 * size_t(w) + 2];
-    }
-    const double inv = 1.0 / double(loop.size());
-    const uint32_t c = V + uint32_t(loops);
-    cap_verts.push_back(float(cx * inv));
-    cap_verts.push_back(float(cy * inv));
-    cap_verts.push_back(float(cz * inv));
-    for (size_t i = 0; i < loop.size(); ++i) {
-      const uint32_t a = loop[i], b = loop[(i + 1) % loop.size()];
-      cap_idx.push_back(b);
-      cap_idx.push_back(a);
-      cap_idx.push_back(c);
-    }
-    ++loops;
-  }
-  return loops;
-}
-
 void srgb_to_linear_table(float out[256]) {
   for (int b = 0; b < 256; ++b) {
     const float c = static_cast<float>(b) / 255.0f;

@@ -16,17 +16,8 @@ int watertight_flag(const uint32_t *tri, size_t ntris, uint64_t *boundary, uint6
 // triangles, equivalent to the reference's test on the de-indexed soup). -2: index out of range.
 int indexed_mesh_watertight(const float *verts, uint32_t V, const uint32_t *idx, uint32_t T);
 
-// Caps that close every boundary loop of an indexed mesh, so that mesh + caps has no boundary.
-// The boundary is the net directed edge chain (an edge used a->b n times and b->a m times
-// contributes n - m copies of a->b); it is split into closed loops, and each loop
-// v0 -> v1 -> ... -> v0 is capped by the fan (v_{i+1}, v_i, c) around its vertex mean c, whose
-// boundary is the loop reversed. cap_verts receives the loop centres (appended after the mesh's V
-// vertices, so cap_idx indexes verts followed by cap_verts). Returns the number of loops.
 // srgbToLinear (src/convert/sdf_baker.cpp:42, voxelize.cpp:12) of every 8-bit channel value
 // b / 255.0f, evaluated on the host as the reference does (so the device reads the same bits).
 void srgb_to_linear_table(float out[256]);
-
-size_t boundary_caps(const float *verts, uint32_t V, const uint32_t *idx, uint32_t T, std::vector<float> &cap_verts,
-                     std::vector<uint32_t> &cap_idx);
 
 }  // namespace sdfb

@@ -99,18 +99,6 @@ void load_tuning(sdfb_ctx *ctx) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// Winding-number caps.
-
-void build_caps(const float *verts, uint32_t V, const uint32_t *idx, uint32_t T, CapBuild &out) {
-  std::vector<float> centres;
-  out.loops = boundary_caps(verts, V, idx, T, centres, out.cidx);
-  out.verts.assign(verts, verts + 3 * size_t(V));
-  out.verts.insert(out.verts.end(), centres.begin(), centres.end());
-  out.pidx.assign(idx, idx + 3 * size_t(T));
-  out.pidx.insert(out.pidx.end(), out.cidx.begin(), out.cidx.end());
-}
-
-// ---------------------------------------------------------------------------------------------
 // Workspace.
 
 bool Workspace::init() {

@@ -622,15 +622,23 @@ sdfb_status sdfb_mesh_register(sdfb_server *srv, const float *verts, uint32_t nu
   if (gs != SDFB_OK) return undo(gs, rc->err);
   r->sign = sign;
   r->watertight = watertight;
-  CapBuild caps;
   size_t cap_bytes = 0;
   if (r->sign == kSignGwn) {
-    build_caps(verts, num_verts, idx, num_tris, caps);
-    r->pV = static_cast<uint32_t>(caps.verts.size() / 3);
-    r->pT = static_cast<uint32_t>(caps.pidx.size() / 3);
-    r->cT = static_cast<uint32_t>(caps.cidx.size() / 3);
+    // caps built on the device in the registration slot's buffers, then copied to exact-size
+    // resident buffers
+    std::vector<PlanMesh> cm(1);
+    cm[0].verts = static_cast<const float *>(r->verts.p);
+    cm[0].idx = static_cast<const uint32_t *>(r->idx.p);
+    cm[0].V = num_verts;
+    cm[0].T = num_tris;
+    cm[0].sign = kSignGwn;
+    const sdfb_status cs = device_caps(rc, st, cm, true);
+    if (cs != SDFB_OK) return undo(cs, rc->err);
+    r->pV = cm[0].pV;
+    r->pT = cm[0].pT;
+    r->cT = cm[0].cT;
     cap_bytes = r->cT ? resident_bytes(r->cT, true) : 0;
-    const uint64_t extra = cap_bytes + caps.verts.size() * 4 + caps.pidx.size() * 4 + caps.cidx.size() * 4;
+    const uint64_t extra = cap_bytes + uint64_t(r->pV) * 12 + uint64_t(r->pT) * 12 + uint64_t(r->cT) * 12;
     {
       std::lock_guard<std::mutex> g(srv->mu);
       if (!srv->make_room(extra)) {
@@ -642,14 +650,12 @@ sdfb_status sdfb_mesh_register(sdfb_server *srv, const float *verts, uint32_t nu
       srv->resident_bytes_used += extra;
       r->bytes += extra;
     }
-    if (!async_alloc(r->pverts, caps.verts.size() * 4, st) || !async_alloc(r->pidx, caps.pidx.size() * 4, st) ||
-        !async_alloc(r->cidx, std::max<size_t>(caps.cidx.size(), 1) * 4, st) ||
-        (cap_bytes && !async_alloc(r->caps, cap_bytes, st)))
+    if (!async_alloc(r->pverts, size_t(r->pV) * 12, st) || !async_alloc(r->pidx, size_t(r->pT) * 12, st) ||
+        !async_alloc(r->cidx, std::max<size_t>(r->cT, 1) * 12, st) || (cap_bytes && !async_alloc(r->caps, cap_bytes, st)))
       return undo(SDFB_ERR_OUT_OF_MEMORY, "device allocation failed");
-    cudaMemcpyAsync(r->pverts.p, caps.verts.data(), caps.verts.size() * 4, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(r->pidx.p, caps.pidx.data(), caps.pidx.size() * 4, cudaMemcpyHostToDevice, st);
-    if (!caps.cidx.empty())
-      cudaMemcpyAsync(r->cidx.p, caps.cidx.data(), caps.cidx.size() * 4, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(r->pverts.p, cm[0].pverts, size_t(r->pV) * 12, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(r->pidx.p, cm[0].pidx, size_t(r->pT) * 12, cudaMemcpyDeviceToDevice, st);
+    if (r->cT) cudaMemcpyAsync(r->cidx.p, cm[0].cidx, size_t(r->cT) * 12, cudaMemcpyDeviceToDevice, st);
   }
   PlanMesh p;
   p.verts = static_cast<const float *>(r->verts.p);
