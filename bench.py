@@ -390,6 +390,18 @@ def hbm_peak_gbs():
         return 6800.0, "fallback 6.8 TB/s"
 
 
+def traffic_record(workload: str):
+    """DRAM bytes of one distance launch of this workload from the committed ncu capture
+    (profiles/traffic.json), or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            rec = json.load(f).get(workload)
+        return None if rec is None else {**rec, "bytes": rec["dram_read_bytes"] + rec["dram_write_bytes"]}
+    except (OSError, ValueError, KeyError):
+        return None
+
+
 def sgemm_peak(torch) -> float:
     """FP32 CUDA-core peak measured as cuBLAS SGEMM (TF32 off), TFLOP/s, best of 5."""
     torch.backends.cuda.matmul.allow_tf32 = False
@@ -928,6 +940,12 @@ def main(argv=None):
     roofline["hbm"] = {"bytes_per_launch": moved, "achieved_gbs": moved / (mean_dist_ms * 1e-3) / 1e9,
                        "peak_gbs": hbm_peak, "frac": moved / (mean_dist_ms * 1e-3) / 1e9 / hbm_peak,
                        "peak_source": hbm_src}
+    tr = traffic_record(args.workload)
+    if tr is not None:
+        # measured DRAM bytes of the pass-A launch (pass B is ~3% of the stage)
+        roofline["traffic"] = tr["bytes"]
+        roofline["traffic_source"] = f"ncu capture of {tr['kernel']} (profiles/traffic.json)"
+        roofline["hbm"]["measured_bytes_per_launch"] = tr["bytes"]
 
     served = None
     if not args.no_serve and args.workload == "batch64" and world == 1:

@@ -22,8 +22,8 @@
 //   pass 1 (FP32, every cell of every winding-number mesh, warp tiles of 4 x 4 x 2): cells
 //     outside the band (|d| > band_voxels * voxel) whose interval [c - e, c + e] lies on one side
 //     of |w| = 0.5 get their sign; the band and undecided cells go to a refine list.
-//   pass 2 (FP64 accumulation and arithmetic, exact caps from the original FP32 vertices, the same
-//     far-field bound per subtree): signs of the refine list; a cell still undecided goes to
+//   pass 2 (FP64 accumulation, exact cap solid angles in FP64 from the original FP32 vertices,
+//     the same FP32 far field): signs of the refine list; a cell still undecided goes to
 //   pass 3 (FP64 sum over every cap triangle of its mesh, one block per cell).
 #include <algorithm>
 #include <cstdint>
@@ -42,7 +42,7 @@ constexpr double kInv4Pi = 0.07957747154594767;
 // bounds cannot move |w| across 0.5; cells far from holes have a margin near 0.5, so the FP64 band
 // pass uses the same bound and only cells it cannot decide go to the direct sum.
 constexpr float kTau32 = 4e-3f;
-constexpr double kTau64 = 4e-3;
+constexpr float kTau64 = 4e-3f;
 
 template <typename T> struct V3 {
   T x, y, z;
@@ -122,11 +122,13 @@ __device__ __forceinline__ float4 leaf_moment(const TriRec *tr, int count) {
 
 // Caps of one mesh seen from q, warp-uniform walk: a subtree every lane can take as its far field
 // (error bound <= tau) adds its dipole term to wex and its bound to eps; otherwise the warp
-// descends, and leaves give exact solid angles. T is the arithmetic type; exact FP64 leaves read
-// the original cap vertices.
+// descends, and leaves give exact solid angles. T is the accumulation type. The far field is
+// evaluated in FP32 either way (its error bound carries FP32's rounding); with EXACT64 the leaves'
+// exact solid angles are FP64, from the original cap vertices, and everything is summed in FP64.
+// q is a cell centre, an FP32 value.
 template <typename T, bool EXACT64>
-__device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, T qx, T qy, T qz, T tau, T &wex,
-                          T &eps, bool &corrupt) {
+__device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, float qx, float qy, float qz, float tau,
+                          T &wex, T &eps, bool &corrupt) {
   const int lane = threadIdx.x & 31;
   int cur = M.cap_root, sp = 0, stk0 = 0, stk1 = 0;
   const long long step_limit = 2ll * M.cap_nodes_n + 64;
@@ -174,13 +176,13 @@ __device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, T qx,
         }
         mom = leaf_moment(M.cap_trec + refs[k], cnts[k]);
       }
-      T val = T(0), err = T(0);
-      const bool far = far_field<T>(qx, qy, qz, n0, n1, n2, k, mom, tau, val, err);
+      float val = 0.0f, err = 0.0f;
+      const bool far = far_field<float>(qx, qy, qz, n0, n1, n2, k, mom, tau, val, err);
       const bool need = active && !far;
       if (!__any_sync(kFull, need)) {
         if (active) {
-          wex += val;
-          eps += err;
+          wex += T(val);
+          eps += T(err);
         }
         continue;
       }
