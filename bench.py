@@ -356,7 +356,8 @@ def run_reference(args, rank, world):
         for step in range(args.steps):
             a, b = cpu_gwn_step(orc, ref, v, i, n, step)
             vox, secs, used = vox + a, secs + b, used + 1
-        what = "occupancy of every cell + FP64 distance on 10^5 and direct FP64 winding number on 256 sampled cells"
+        what = ("occupancy of every cell + FP64 distance on 10^5 and direct FP64 winding number on 256 sampled "
+                "cells, each step's per-cell cost scaled to the whole grid")
     else:
         for w in range(min(args.warmup, 1)):
             cpu_sample(meshes, 1.0, 1000 + w, orc, ref)

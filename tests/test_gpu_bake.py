@@ -171,6 +171,28 @@ def test_displaced_sphere_full_size(ctx, oracle):
     assert flat[(128 * 256 + 128) * 256 + 128] < 0 and flat[0] > 0
 
 
+def test_million_triangle_torus_every_cell(ctx, oracle):
+    """The heaviest meshes of the batch are 1M-triangle tori: one (1,048,576 triangles) at 128^3
+    against FP64 on every cell -- occupancy bit-exact, distance within 1e-5 of the diagonal, sign
+    exact outside one voxel -- through the single-mesh path and inside a batch with a small mesh."""
+    import sdfb
+    from sdfb import meshgen as mg
+    v, i = mg.displaced_torus(1024, 512, 0.3, 0.1, 1114)
+    assert len(i) == 1 << 20
+    n = (128, 128, 128)
+    origin, voxel = (-0.5,) * 3, 1.0 / 128
+    g = sdfb.make_grid(origin, voxel, n)
+    dist, occ = ctx.bake(v, i, g, sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY))
+    err, _, _ = check_bake(oracle, v, i, origin, voxel, n, dist, occ)
+    assert err <= DIST_TOL
+    small_v, small_i = mg.displaced_icosphere(3, 0.3, 5)
+    gs = sdfb.make_grid(origin, 1.0 / 32, (32, 32, 32))
+    (bd, _), (bo, _) = ctx.bake_batch([(v, i), (small_v, small_i)], [g, gs],
+                                      sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY))
+    assert np.array_equal(bo, occ)
+    assert np.abs(bd - dist).max() <= DIST_TOL * np.sqrt(3)
+
+
 def test_grid_edge_cases(ctx, oracle):
     import sdfb
     tri_v = np.array([[0.1, 0.1, 0.1], [0.3, 0.1, 0.2], [0.1, 0.35, 0.3]], np.float32)
