@@ -439,8 +439,11 @@ def percentile(xs, p):
     return ys[k]
 
 
-def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, repeat=0.3, workers=64,
-                 wave_log2=27, max_inflight=64, closed_loop=False):
+_SLOT_BUFS: list = []
+
+
+def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, repeat=0.3, workers=128,
+                 wave_log2=28, max_inflight=128, closed_loop=False):
     """The Poisson serving stream. Returns the served record and the request list (for plain).
     closed_loop: no arrival times -- each of the `workers` clients submits its next request as soon
     as its last one returns, for `seconds` (the server's capacity at that concurrency); latency is
@@ -459,14 +462,14 @@ def serve_stream(sdfb, ctx, torch, base_meshes, seconds, seed=77, rate=200.0, re
             key = (int(rng.integers(len(base_meshes))), tuple(rng.uniform(-0.03, 0.03, 3).astype(np.float32)))
             news.append(key)
         reqs.append((t, key, n))
-    # pinned output slots, sized for the largest grid
+    # pinned output slots, sized for the largest grid (allocated once, shared by the streams)
     max_cells = 256 ** 3
     slots = queue.Queue()
-    slot_bufs = []
+    while len(_SLOT_BUFS) < workers:
+        _SLOT_BUFS.append((torch.empty(max_cells, dtype=torch.float32).pin_memory().numpy(),
+                           torch.empty(max_cells, dtype=torch.uint8).pin_memory().numpy()))
+    slot_bufs = _SLOT_BUFS[:workers]
     for k in range(workers):
-        d = torch.empty(max_cells, dtype=torch.float32).pin_memory().numpy()
-        o = torch.empty(max_cells, dtype=torch.uint8).pin_memory().numpy()
-        slot_bufs.append((d, o))
         slots.put(k)
     results = [None] * len(reqs)
     srv = sdfb.Server(ctx, hbm_budget_bytes=150 << 30, max_inflight=max_inflight, wave_voxels_log2=wave_log2)
@@ -963,7 +966,7 @@ def main(argv=None):
                               closed_loop=True)
         served["saturation"] = {k: sat[k] for k in ("requests", "completed", "dropped", "voxels_per_s", "p50_ms",
                                                     "p99_ms", "mean_ms", "seconds")}
-        served["saturation"]["note"] = ("closed loop: 64 clients, each submits its next request when the last "
+        served["saturation"]["note"] = ("closed loop: 128 clients, each submits its next request when the last "
                                         "one returns; latency from submission")
         stage(f"saturation: {sat['voxels_per_s'] / 1e6:.0f} M voxels/s")
 

@@ -304,8 +304,8 @@ typedef struct sdfb_server sdfb_server;
 typedef struct sdfb_server_opts {
   uint32_t struct_size;
   uint64_t hbm_budget_bytes; /* admission budget for resident meshes + in-flight jobs */
-  int32_t max_inflight;      /* jobs on the device at once, default 64 */
-  int32_t wave_voxels_log2;  /* most work per wave (log2 voxels), default 27; a wave takes what is queued */
+  int32_t max_inflight;      /* jobs on the device at once, default 128 */
+  int32_t wave_voxels_log2;  /* most work per wave (log2 voxels), default 28; a wave takes what is queued */
   int32_t reserved[8];
 } sdfb_server_opts;
 

