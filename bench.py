@@ -604,24 +604,6 @@ def plain_stream(sdfb, ctx, base_meshes, reqs, seconds):
 # Per-config records (c1-c3): GPU time, FP64 precision, mismatches, CPU bake of the same mesh
 
 
-def vpl_of_tile(tile_used: int) -> int:
-    """Cells per lane of a distance tile shape (sdfb_opts.tile numbering, 1-based)."""
-    shapes = {1: (4, 4, 2), 2: (8, 4, 1), 3: (4, 4, 4), 4: (8, 4, 2), 5: (4, 4, 8), 6: (8, 4, 4)}
-    tx, ty, tz = shapes.get(int(tile_used), (4, 4, 8))
-    return tz // (32 // (tx * ty))
-
-
-def executed_flops(st) -> float:
-    """FP32 flops of the distance tests as the kernel executes them: the terms a lane forms once for
-    its VPL cells (the x and y parts of a box distance, of the plane height and of the in-plane
-    coordinates) are counted once per lane. Per cell: box 4 + 7/VPL, plane 4 + 5/VPL, rectangle
-    10 + 6/VPL, full test 31 (the counts behind sdfb_stats.flops_distance charge every cell 11, 9,
-    16 and 31)."""
-    vpl = vpl_of_tile(st.tile_used)
-    return (st.box_tests * (4 + 7 / vpl) + st.plane_tests * (4 + 5 / vpl) + st.rect_tests * (10 + 6 / vpl)
-            + st.tri_tests * 31.0)
-
-
 def gpu_single(sdfb, ctx, torch, stream, flush, v, i, n, sign, reps=5):
     """Single-mesh bake on device buffers (sdfb_bake_device), median of `reps` timed bakes after two
     warm-ups, plus the same bake end to end from host buffers (sdfb_bake, pinned outputs). Returns
@@ -923,8 +905,10 @@ def main(argv=None):
     # ---- roofline of the distance kernel ----
     peak = sgemm_peak(torch)
     stage(f"SGEMM peak {peak:.1f} TFLOP/s")
-    flops_count = cst.flops_distance
-    flops = executed_flops(cst)
+    # as executed (terms a lane shares between its cells counted once), and the previous counting
+    # that charges every cell for them (box 11, plane 9, rectangle 16, full test 31 flops)
+    flops = float(cst.flops_distance)
+    flops_count = (cst.box_tests * 11.0 + cst.plane_tests * 9.0 + cst.rect_tests * 16.0 + cst.tri_tests * 31.0)
     mean_dist_ms = statistics.mean(dist_ms)
     achieved = flops / (mean_dist_ms * 1e-3) / 1e12
     roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
