@@ -47,6 +47,50 @@ def test_gwn_sign_matches_fp64_oracle(ctx, oracle, seed, n):
     assert bad_near <= max(2, near.sum() // 1000)
 
 
+def _holes_meeting_at_vertices(level=3, seed=8):
+    """A displaced icosphere with (a) two holes that share exactly one vertex (a boundary vertex with
+    two arriving and two leaving boundary half-edges, where the cap loops can be split either way),
+    (b) every triangle around another vertex removed (one long loop), and (c) a second sphere
+    inside the first, with one triangle removed."""
+    from sdfb import meshgen as mg
+    v, f = mg.displaced_icosphere(level, 0.3, seed)
+    f = np.asarray(f, np.int64)
+    # (a) two faces meeting only at vertex x
+    x = int(f[0, 0])
+    around = [t for t in range(len(f)) if x in f[t]]
+    a = around[0]
+    b = next(t for t in around[1:] if len(set(f[t]) & set(f[a])) == 1)
+    # (b) the fan of the vertex farthest from x
+    y = int(np.argmax(np.linalg.norm(np.asarray(v, np.float64) - np.asarray(v[x], np.float64), axis=1)))
+    fan = [t for t in range(len(f)) if y in f[t]]
+    drop = set([a, b] + fan)
+    keep = np.array([t for t in range(len(f)) if t not in drop])
+    outer_v, outer_f = v, f[keep]
+    iv, ifc = mg.displaced_icosphere(2, 0.12, seed + 1, center=(0.05, 0.0, 0.02))
+    ifc = np.asarray(ifc, np.int64)[1:]
+    return mg.concat([(outer_v, outer_f), (iv, ifc)])
+
+
+def test_device_caps_on_loops_that_share_vertices(ctx, oracle):
+    """The caps built on the device close loops that meet at a vertex and long loops; every cell
+    outside the band gets the FP64 winding number's sign."""
+    import sdfb
+    v, f = _holes_meeting_at_vertices()
+    n = 48
+    origin, voxel = (-0.5,) * 3, 1.0 / n
+    grid = sdfb.make_grid(origin, voxel, (n, n, n))
+    dist, _ = ctx.bake(v, f, grid, sdfb.make_opts(sign_mode=sdfb.SIGN_GWN))
+    flat = dist.reshape(-1)
+    d64 = oracle.distance(v, f, origin, voxel, (n, n, n))
+    w = oracle.gwn(v, f, origin, voxel, (n, n, n))
+    far = (d64 > voxel) & (np.abs(np.abs(w) - 0.5) > 1e-6)
+    assert far.sum() > 0.9 * flat.size
+    bad = np.count_nonzero((flat[far] < 0) != (np.abs(w[far]) > 0.5))
+    assert bad == 0, f"{bad} sign mismatches outside the band"
+    # both spheres' interiors are inside (the holes do not open them)
+    assert flat[(24 * n + 24) * n + 27] < 0
+
+
 def test_gwn_equals_parity_on_closed_mesh(ctx):
     import sdfb
     from sdfb import meshgen as mg
