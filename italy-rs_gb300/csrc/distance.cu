@@ -251,14 +251,14 @@ __device__ __forceinline__ bool walk(const Node *__restrict__ nodes, const DistT
     const Node *np = nodes + node;
     const float4 n0 = __ldg(&np->n0), n1 = __ldg(&np->n1), n2 = __ldg(&np->n2);
     const int4 n3 = __ldg(&np->n3);
-    float d0[VPL], d1[VPL];
+    // Only the votes stay live: when the near child is a leaf, the far child's box is read again
+    // (an L1 hit) and re-tested after it, which keeps the per-cell distances out of the registers
+    // across the leaf test (fewer spills: 64-mesh batch 249 -> 244 ms).
     bool w0 = false, w1 = false;
 #pragma unroll
     for (int v = 0; v < VPL; ++v) {
-      d0[v] = box_dist2(px, py, pz[v], n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
-      d1[v] = box_dist2(px, py, pz[v], n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
-      w0 |= d0[v] < best[v];
-      w1 |= d1[v] < best[v];
+      w0 |= box_dist2(px, py, pz[v], n0.x, n0.y, n0.z, n0.w, n1.x, n1.y) < best[v];
+      w1 |= box_dist2(px, py, pz[v], n1.z, n1.w, n2.x, n2.y, n2.z, n2.w) < best[v];
     }
     if (COUNT) ws.box_tests += 2 * kWarp * VPL;
     w0 = __any_sync(kFull, w0) && n3.z >= 0;
@@ -294,8 +294,12 @@ __device__ __forceinline__ bool walk(const Node *__restrict__ nodes, const DistT
       test_leaf<VPL, COUNT>(tris, num_tris, near_ref, near_cnt, px, py, pz, best, ws);
       if (far_w) {
         bool w = false;
+        const Node *fp = nodes + node;
+        const float4 f0 = __ldg(&fp->n0), f1 = __ldg(&fp->n1), f2 = __ldg(&fp->n2);
 #pragma unroll
-        for (int v = 0; v < VPL; ++v) w |= (second_first ? d0[v] : d1[v]) < best[v];
+        for (int v = 0; v < VPL; ++v)
+          w |= (second_first ? box_dist2(px, py, pz[v], f0.x, f0.y, f0.z, f0.w, f1.x, f1.y)
+                             : box_dist2(px, py, pz[v], f1.z, f1.w, f2.x, f2.y, f2.z, f2.w)) < best[v];
         far_w = __any_sync(kFull, w);
       }
     }
