@@ -43,6 +43,12 @@ using namespace sdfb;
 namespace {
 
 constexpr int kRegSlots = 4;  // meshes registered (uploaded, gated, built) at the same time
+// While a registration is in progress, waves launch their persistent kernels on kReserveSms fewer
+// SMs and each wave's work waits for the previous wave's (kSerialWaves): a wave's persistent
+// distance kernel otherwise holds every SM until it ends, and each step of a registration (gate,
+// caps, hierarchy, separated by host reads) would wait for the waves queued ahead of it.
+constexpr int kReserveSms = 8;
+constexpr bool kSerialWaves = true;
 
 double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -130,6 +136,7 @@ struct Wave {
   sdfb_opts opts{};
   uint64_t bytes = 0;  // budget charge of this wave
   bool busy = false;
+  bool lean = false;  // launched while a registration was in progress
 };
 
 bool is_pinned(const void *p) {
@@ -176,6 +183,8 @@ struct sdfb_server {
   uint64_t budget = 0, resident_bytes_used = 0, inflight_bytes = 0;
   int max_inflight = 128, inflight = 0;
   uint64_t wave_cells = 1ull << 27;
+  cudaEvent_t last_wave_done = nullptr;  // the last launched wave's completion (serial waves)
+  int all_sms = 0;
   std::string err;
   cudaMemPool_t pool = nullptr;
 
@@ -195,11 +204,19 @@ struct sdfb_server {
 
 namespace {
 
-std::unique_ptr<sdfb_ctx> make_private_ctx(int device, int num_sms, const sdfb_ctx *tuned) {
+// high_priority: the stream's pending blocks are scheduled before those of default-priority
+// streams (the waves') as SMs free up.
+std::unique_ptr<sdfb_ctx> make_private_ctx(int device, int num_sms, const sdfb_ctx *tuned, bool high_priority = false) {
   auto c = std::make_unique<sdfb_ctx>();
   c->device = device;
   c->num_sms = num_sms;
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+  int least = 0, greatest = 0;
+  if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) {
+    cudaGetLastError();
+    greatest = least = 0;
+  }
+  if (cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, high_priority ? greatest : least) != cudaSuccess)
+    return nullptr;
   if (!c->ws.init()) return nullptr;
   std::memcpy(c->tuned_leaf, tuned->tuned_leaf, sizeof c->tuned_leaf);
   std::memcpy(c->tuned_tile, tuned->tuned_tile, sizeof c->tuned_tile);
@@ -297,6 +314,8 @@ bool sdfb_server::launch_wave(Wave &w) {
   }
   w.opts = w.reqs[0]->opts;
   w.opts.sign_mode = SDFB_SIGN_AUTO;  // per-mesh signs are already resolved in the plan
+  sched->num_sms = w.lean ? std::max(1, all_sms - kReserveSms) : all_sms;
+  if (kSerialWaves && w.lean && last_wave_done) cudaStreamWaitEvent(w.stream, last_wave_done, 0);
   sdfb_status s = enqueue_batch(sched.get(), w.ws, w.stream, plan, w.opts, false, w.state);
   if (s != SDFB_OK) {
     for (Request *r : w.reqs) r->status = s;
@@ -304,6 +323,7 @@ bool sdfb_server::launch_wave(Wave &w) {
   }
   enqueue_readback(w);
   cudaEventRecord(w.done, w.stream);
+  last_wave_done = w.done;
   return true;
 }
 
@@ -418,8 +438,12 @@ void sdfb_server::run() {
           inflight++;
           cells += n;
         }
-        if (!free_slot->reqs.empty()) free_slot->busy = true;
-        else free_slot = nullptr;
+        if (!free_slot->reqs.empty()) {
+          free_slot->busy = true;
+          free_slot->lean = std::any_of(reg_busy.begin(), reg_busy.end(), [](char b) { return b != 0; });
+        } else {
+          free_slot = nullptr;
+        }
       } else {
         free_slot = nullptr;
       }
@@ -460,10 +484,11 @@ sdfb_status sdfb_server_create(sdfb_ctx *ctx, const sdfb_server_opts *opts, sdfb
   // of 2^27 voxels 973 M voxels/s; 128 and 2^28 1042 M (fuller waves, fewer tails).
   srv->max_inflight = o.max_inflight > 0 ? o.max_inflight : 128;
   srv->wave_cells = 1ull << (o.wave_voxels_log2 > 10 && o.wave_voxels_log2 < 36 ? o.wave_voxels_log2 : 28);
+  srv->all_sms = ctx->num_sms;
   srv->sched = make_private_ctx(ctx->device, ctx->num_sms, ctx);
   if (!srv->sched) return SDFB_ERR_CUDA;
   for (int k = 0; k < kRegSlots; ++k) {
-    srv->regs.push_back(make_private_ctx(ctx->device, ctx->num_sms, ctx));
+    srv->regs.push_back(make_private_ctx(ctx->device, ctx->num_sms, ctx, true));
     if (!srv->regs.back()) return SDFB_ERR_CUDA;
   }
   srv->reg_busy.assign(kRegSlots, 0);
