@@ -148,6 +148,9 @@ struct sdfb_ctx {
   int tuned_tile[32][8];
   int tuned_stack[32][8];
   int tuned_budget[32][8];  // distance pass: steps before a tile is deferred (0 = never)
+  // Batch-wide override for bakes of more than one mesh ("batch tile stack budget" in the table;
+  // tile -1 = none): a batch otherwise takes the bucket of its mesh with the most cells.
+  int batch_tile = -1, batch_stack = 64, batch_budget = 0;
 
   ~sdfb_ctx();
   DevBuf *all_bufs(int i);

@@ -48,7 +48,9 @@ thread_local uint64_t t_alloc_cap = 0;
 // Tuned defaults: leaf size, tile shape, stack depth and the distance pass's deferral budget per
 // (log2 triangles, log2 grid edge - 4). The table is written by the autotuner
 // (italy-rs_gb300/sdfb/autotune.py) as lines "tri_bucket grid_bucket leaf tile stack [budget]" in
-// italy-rs_gb300/tuning/gb300.tsv next to lib/; SDFB_TUNING names another file.
+// italy-rs_gb300/tuning/gb300.tsv next to lib/; SDFB_TUNING names another file. An optional line
+// "batch tile stack budget" (written by the tuner's batch mode) sets the tile shape, stack depth
+// and budget of every bake of more than one mesh.
 
 int bucket_tris(uint64_t T) {
   int b = 0;
@@ -87,6 +89,14 @@ void load_tuning(sdfb_ctx *ctx) {
   char line[256];
   while (std::fgets(line, sizeof line, f)) {
     int tb, nb, leaf, tile, stack, budget = -1;
+    if (std::sscanf(line, "batch %d %d %d", &tile, &stack, &budget) == 3) {
+      if (tile >= 0 && tile < tile_shape_count() && (stack == 32 || stack == 64) && budget >= 0) {
+        ctx->batch_tile = tile;
+        ctx->batch_stack = stack;
+        ctx->batch_budget = budget;
+      }
+      continue;
+    }
     if (line[0] == '#' || std::sscanf(line, "%d %d %d %d %d %d", &tb, &nb, &leaf, &tile, &stack, &budget) < 5)
       continue;
     if (tb < 0 || tb >= 32 || nb < 0 || nb >= 8) continue;
@@ -160,9 +170,13 @@ void make_layout(sdfb_ctx *ctx, const std::vector<PlanMesh> &ms, const sdfb_opts
         uint64_t(ms[big].grid.nx) * ms[big].grid.ny * ms[big].grid.nz)
       big = m;
   const int tb = bucket_tris(ms[big].T), nb = bucket_grid(ms[big].grid);
-  L.tile_id = (o.tile >= 1 && o.tile <= tile_shape_count()) ? o.tile - 1 : ctx->tuned_tile[tb][nb];
-  L.stack = (o.stack_depth == 32 || o.stack_depth == 64) ? o.stack_depth : ctx->tuned_stack[tb][nb];
-  L.step_budget = o.step_budget > 0 ? o.step_budget : (o.step_budget < 0 ? 0 : ctx->tuned_budget[tb][nb]);
+  const bool batch = M > 1 && ctx->batch_tile >= 0;  // the table's batch-wide line, when it has one
+  L.tile_id = (o.tile >= 1 && o.tile <= tile_shape_count()) ? o.tile - 1
+                                                           : (batch ? ctx->batch_tile : ctx->tuned_tile[tb][nb]);
+  L.stack = (o.stack_depth == 32 || o.stack_depth == 64) ? o.stack_depth
+                                                         : (batch ? ctx->batch_stack : ctx->tuned_stack[tb][nb]);
+  L.step_budget = o.step_budget > 0 ? o.step_budget
+                                    : (o.step_budget < 0 ? 0 : (batch ? ctx->batch_budget : ctx->tuned_budget[tb][nb]));
   L.resident = ms[0].bvh != nullptr;
   uint64_t T_total = 0;
   for (const auto &p : ms) T_total += p.T;

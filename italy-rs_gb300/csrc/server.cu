@@ -222,6 +222,9 @@ std::unique_ptr<sdfb_ctx> make_private_ctx(int device, int num_sms, const sdfb_c
   std::memcpy(c->tuned_tile, tuned->tuned_tile, sizeof c->tuned_tile);
   std::memcpy(c->tuned_stack, tuned->tuned_stack, sizeof c->tuned_stack);
   std::memcpy(c->tuned_budget, tuned->tuned_budget, sizeof c->tuned_budget);
+  c->batch_tile = tuned->batch_tile;
+  c->batch_stack = tuned->batch_stack;
+  c->batch_budget = tuned->batch_budget;
   return c;
 }
 

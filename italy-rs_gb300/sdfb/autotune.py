@@ -19,7 +19,15 @@ nearest measured one and writes "tri_bucket grid_bucket leaf tile stack budget" 
 0-based, budget 0 = never) that
 the library reads at context creation (tuning/gb300.tsv beside lib/, or the file SDFB_TUNING names).
 
+A batch takes its tile shape, stack depth and budget from the bucket of its mesh with the most
+cells. The batch mode (--batch) times a 64-mesh batch (1e3..1e6 triangles, 32^3..256^3 grids) with
+those choices and under a coordinate descent over batch-wide (tile, stack, budget) settings; when
+the best beats the table's choice by more than BATCH_GAIN it writes a "batch tile stack budget"
+line into the table, which the library then uses for every bake of more than one mesh, and
+otherwise it records the comparison as a comment.
+
     python italy-rs_gb300/sdfb/autotune.py [--out PATH] [--quick]
+    python italy-rs_gb300/sdfb/autotune.py --batch [--out PATH]
 """
 from __future__ import annotations
 
@@ -44,6 +52,7 @@ SWEEP = [(3, 32), (3, 64), (3, 128), (3, 256), (4, 64), (4, 128), (4, 256), (5, 
          (5, 256), (5, 512), (6, 32), (6, 64), (6, 128), (6, 256), (6, 512), (7, 32), (7, 64), (7, 128),
          (7, 256), (7, 512), ("torus128k", 128), ("torus128k", 256), ("torus1m", 128), ("torus1m", 256)]
 QUICK = [(4, 128), (6, 256), (7, 256)]
+BATCH_GAIN = 0.02  # a batch-wide line is written only when it saves more than this fraction
 TORI = {"torus128k": (512, 128), "torus1m": (1024, 512)}  # nu x nv quads, 2 nu nv triangles
 
 
@@ -94,6 +103,72 @@ def write_table(path: str, table: dict, measured: dict, times: dict, header: lis
             f.write(f"{tb} {nb} {leaf} {tile - 1} {stack} {max(budget, 0)}{note}\n")
 
 
+def write_batch_line(path: str, params, note: str):
+    """Replaces the table's batch line (and batch comments) by `params` = (tile 1-based, stack,
+    budget) or, when params is None, by the comment `note` alone."""
+    lines = []
+    if os.path.exists(path):
+        with open(path) as f:
+            lines = [l for l in f.read().splitlines() if not l.startswith("batch ") and not l.startswith("# batch:")]
+    if params is None:
+        lines.append(f"# batch: {note}")
+    else:
+        tile, stack, budget = params
+        lines.append(f"batch {tile - 1} {stack} {max(budget, 0)}  # {note}")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def tune_batch(time_batch, log=print):
+    """Coordinate descent over batch-wide (tile, stack, budget) from the table's own choice.
+    time_batch(params or None) -> ms. Returns (best params or None, best ms, table ms)."""
+    cache = {}
+
+    def t(p):
+        if p not in cache:
+            cache[p] = time_batch(p)
+        return cache[p]
+
+    table_ms = t(None)
+    best, best_ms = None, table_ms
+    cur = (START[1], START[2], START[3])
+    for axis, values in ((0, TILES), (1, STACKS), (2, BUDGETS), (0, TILES)):
+        for v in values:
+            p = list(cur)
+            p[axis] = v
+            p = tuple(p)
+            if t(p) < t(cur):
+                cur = p
+    if t(cur) < best_ms:
+        best, best_ms = cur, t(cur)
+    log(f"    batch: {len(cache)} configurations, table {table_ms:.3f} ms, best batch-wide {cur} {t(cur):.3f} ms")
+    return best, best_ms, table_ms
+
+
+def _time_batch(ctx, torch, sdfb, devm, grids, outs, params, reps: int) -> float:
+    tile, stack, budget = params if params is not None else (0, 0, 0)
+    opts = sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY, tile=tile, stack_depth=stack, step_budget=budget)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(128 << 20, dtype=torch.float32, device="cuda")  # 512 MB > L2
+
+    def step():
+        ctx.bake_batch_device(devm, grids, opts, outs[0], outs[1], stream.cuda_stream)
+
+    step()
+    step()
+    times = []
+    for _ in range(reps):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    times.sort()
+    return times[len(times) // 2]
+
+
 def _time_bake(ctx, torch, sdfb, dev, grid, params, reps: int) -> float:
     leaf, tile, stack, budget = params
     opts = sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY, leaf_size=leaf, tile=tile, stack_depth=stack,
@@ -141,6 +216,7 @@ def main(argv=None):
     ap.add_argument("--out", default=DEFAULT_OUT)
     ap.add_argument("--quick", action="store_true", help="three buckets only")
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--batch", action="store_true", help="tune batch-wide settings against the table at --out")
     args = ap.parse_args(argv)
 
     sys.path.insert(0, os.path.dirname(HERE))
@@ -149,6 +225,30 @@ def main(argv=None):
 
     import sdfb
     from sdfb import meshgen
+
+    if args.batch:
+        os.environ["SDFB_TUNING"] = args.out  # the batch is timed against this table's choices
+        write_batch_line(args.out, None, "being tuned")  # no batch line while timing
+        ctx = sdfb.Context(0)
+        meshes = meshgen.batch_meshes(64, seed=2024)
+        grids = [sdfb.make_grid((-0.5,) * 3, 1.0 / n, (n, n, n)) for _, _, n in meshes]
+        dv = [torch.from_numpy(np.ascontiguousarray(v, np.float32)).cuda() for v, _, _ in meshes]
+        di = [torch.from_numpy(np.ascontiguousarray(f, np.int32)).cuda() for _, f, _ in meshes]
+        dd = [torch.empty(g.cells, dtype=torch.float32, device="cuda") for g in grids]
+        do = [torch.empty(g.cells, dtype=torch.uint8, device="cuda") for g in grids]
+        devm = [(a.data_ptr(), len(v), b.data_ptr(), len(f)) for a, b, (v, f, _) in zip(dv, di, meshes)]
+        outs = ([d.data_ptr() for d in dd], [o.data_ptr() for o in do])
+        best, best_ms, table_ms = tune_batch(
+            lambda p: _time_batch(ctx, torch, sdfb, devm, grids, outs, p, args.reps))
+        stamp = f"{torch.cuda.get_device_name(0)}, {datetime.date.today().isoformat()}, 64-mesh batch"
+        if best is not None and best_ms < (1.0 - BATCH_GAIN) * table_ms:
+            write_batch_line(args.out, best, f"{stamp}: {best_ms:.1f} ms against {table_ms:.1f} ms per mesh bucket")
+        else:
+            write_batch_line(args.out, None, f"{stamp}: the per-bucket choice kept ({table_ms:.1f} ms; best "
+                                             f"batch-wide {best_ms:.1f} ms)")
+        print(f"wrote {args.out}")
+        ctx.close()
+        return
 
     os.environ["SDFB_TUNING"] = os.devnull  # tune from the built-in defaults, not an older table
     ctx = sdfb.Context(0)

@@ -139,3 +139,39 @@ def test_pinned_outputs_are_written_in_place(ctx):
                                alloc=lambda shape, dt: torch.empty(int(np.prod(shape)), dtype=tdt[dt])
                                .pin_memory().numpy().reshape(shape))
     assert g2.shape == g0.shape and np.array_equal(d2, d0) and np.array_equal(o2, o0)
+
+
+def test_batch_line_of_the_tuning_table(tmp_path, monkeypatch):
+    """A "batch tile stack budget" line in the tuning table sets those for every bake of more than
+    one mesh; single-mesh bakes keep the per-bucket rows; the grids match the context without it."""
+    import sdfb
+    table = tmp_path / "t.tsv"
+    table.write_text("# test table\n0 0 4 0 64 1024\nbatch 1 32 0\n")
+    monkeypatch.setenv("SDFB_TUNING", str(table))
+    ctx_b = sdfb.Context(0)
+    table.write_text("# test table\n0 0 4 0 64 1024\n")
+    ctx_p = sdfb.Context(0)
+    try:
+        meshes, grids = small_batch(seed=9, count=4)
+        opts = sdfb.make_opts(sign_mode=sdfb.SIGN_PARITY)
+        sts = []
+        outs = []
+        for c in (ctx_b, ctx_p):
+            st = sdfb.Stats()
+            st.struct_size = sdfb.C.sizeof(sdfb.Stats)
+            outs.append(c.bake_batch(meshes, grids, opts, stats=st))
+            sts.append(st)
+        assert (sts[0].tile_used, sts[0].stack_used) == (2, 32)
+        assert sts[1].tile_used == 3  # the built-in default (tile id 2 + 1) for buckets the table lacks
+        (db, ob), (dp, op) = outs
+        for a, b in zip(ob, op):
+            assert np.array_equal(a, b)
+        for a, b in zip(db, dp):
+            assert np.abs(a - b).max() <= 4e-7 and np.array_equal(a < 0, b < 0)
+        st = sdfb.Stats()
+        st.struct_size = sdfb.C.sizeof(sdfb.Stats)
+        ctx_b.bake(*meshes[0], grids[0], opts, stats=st)
+        assert st.tile_used == 3  # one mesh: no batch line
+    finally:
+        ctx_b.close()
+        ctx_p.close()
