@@ -200,7 +200,7 @@ __device__ __forceinline__ bool column_crossing(f3 a, f3 b, f3 c, float px, floa
 //   r0 = (v0, 1/|e1|^2)    e1 = v1 - v0
 //   r1 = (e1, 1/|e2|^2)    e2 = v2 - v0
 //   r2 = (e2, 1/|e3|^2)    e3 = v2 - v1
-//   r3 = (n,  1/|n|^2)     n = e1 x e2; 1/|n|^2 = 0 marks a degenerate triangle
+//   r3 = (n,  |n|)         n = e1 x e2 (|n| is twice the area)
 struct TriRec {
   float4 r0, r1, r2, r3;
 };

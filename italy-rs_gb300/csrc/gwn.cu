@@ -23,7 +23,9 @@
 //     outside the band (|d| > band_voxels * voxel) whose interval [c - e, c + e] lies on one side
 //     of |w| = 0.5 get their sign; the band and undecided cells go to a refine list.
 //   pass 2 (FP64 accumulation, exact cap solid angles in FP64 from the original FP32 vertices,
-//     the same FP32 far field): signs of the refine list; a cell still undecided goes to
+//     the same FP32 far field): signs of the refine list, first with coarse subtrees (kTau64),
+//     then the cells that stay undecided again with fine ones (kTau64Fine); a cell still
+//     undecided goes to
 //   pass 3 (FP64 sum over every cap triangle of its mesh, one block per cell).
 #include <algorithm>
 #include <cstdint>
@@ -42,10 +44,13 @@ constexpr double kInv4Pi = 0.07957747154594767;
 // bounds cannot move |w| across 0.5, and most cells have a margin near 0.5, so the FP32 pass takes
 // coarse subtrees (500k-triangle soup at 512^3, sign stage: 4e-3 sr 256 ms, 2e-2 155 ms, 0.1
 // 116 ms, 0.3 123 ms, with the same signs; 0.1 leaves 1.5% more cells to the FP64 pass). The FP64
-// band pass takes finer ones (4e-3: 116 ms, 2e-2: 87 ms and 1,712 cells left to the direct sum,
-// 0.1: 132 ms and 10,599), and only cells it cannot decide go to the direct sum.
+// band pass runs twice: coarse subtrees first, then fine ones for the cells still undecided, and
+// only cells neither decides go to the direct sum (one pass at 2e-2: sign stage 87 ms, ~950 cells
+// summed directly; 0.1 then 5e-3: 74 ms, ~500; 0.3 then 1e-2: 71 ms, ~850; 5e-2 then 5e-4: 98 ms,
+// ~120 -- the direct sum costs ~10 us a cell, the fine walk little, the coarse walk most).
 constexpr float kTau32 = 1e-1f;
-constexpr float kTau64 = 2e-2f;
+constexpr float kTau64 = 3e-1f;
+constexpr float kTau64Fine = 1e-2f;
 
 template <typename T> struct V3 {
   T x, y, z;
@@ -70,10 +75,11 @@ struct GwnArgs {
   const float *col_z;
   const int8_t *col_s;
   float band_voxels;
-  uint64_t *refine;
+  uint64_t *refine;  // pass 1 -> pass 2 (coarse); reused for pass 2 (fine) -> pass 3
   unsigned long long *refine_count;
-  uint64_t *direct;
+  uint64_t *direct;  // pass 2 (coarse) -> pass 2 (fine)
   unsigned long long *direct_count;
+  unsigned long long *final_count;  // cells for pass 3, listed in refine
   unsigned long long *tile_counter;
   uint32_t *err;
 };
@@ -110,7 +116,8 @@ __device__ __forceinline__ bool far_field(T qx, T qy, T qz, const float4 &n0, co
   return true;
 }
 
-// (D, A) of a leaf's cap triangles (D = half the sum of their edge cross products).
+// (D, A) of a leaf's cap triangles (D = half the sum of their edge cross products, A = half the
+// sum of their lengths, which the records hold).
 __device__ __forceinline__ float4 leaf_moment(const TriRec *tr, int count) {
   float4 m = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   for (int j = 0; j < count; ++j) {
@@ -118,9 +125,34 @@ __device__ __forceinline__ float4 leaf_moment(const TriRec *tr, int count) {
     m.x += 0.5f * r3.x;
     m.y += 0.5f * r3.y;
     m.z += 0.5f * r3.z;
-    m.w += 0.5f * sqrtf(r3.x * r3.x + r3.y * r3.y + r3.z * r3.z);
+    m.w += 0.5f * r3.w;
   }
   return m;
+}
+
+// FP32 far field with one reciprocal square root per distance and one approximate reciprocal for
+// the bound (each within 2 ulp, far inside the kRel margin the bound carries); the acceptance
+// test err <= tau is taken as A 2 rho <= tau g^3 with a 1e-6 margin, without a division.
+constexpr bool kFastFarField = true;
+__device__ __forceinline__ bool far_field_fast(float qx, float qy, float qz, const float4 &n0, const float4 &n1,
+                                               const float4 &n2, int which, const float4 &m, float tau, float &val,
+                                               float &err) {
+  const float cx = which ? n1.z : n0.x, cy = which ? n1.w : n0.y, cz = which ? n2.x : n0.z;
+  const float ex = which ? n2.y : n0.w, ey = which ? n2.z : n1.x, ez = which ? n2.w : n1.y;
+  const float dx = cx - qx, dy = cy - qy, dz = cz - qz;
+  const float r2 = dx * dx + dy * dy + dz * dz;
+  const float rho2 = ex * ex + ey * ey + ez * ez;
+  if (!(r2 > 4.0f * rho2)) return false;
+  const float ir = rsqrtf(r2);
+  const float rho = rho2 > 0.0f ? rho2 * rsqrtf(rho2) : 0.0f;
+  const float g = r2 * ir - rho;
+  const float g3 = g * g * g;
+  const float lim = m.w * 2.0f * rho;
+  if (!(g3 > 1e-30f) || !(lim <= tau * (1.0f - 1e-6f) * g3)) return false;
+  val = (m.x * dx + m.y * dy + m.z * dz) * (ir * ir * ir);
+  constexpr float kRel = 1e-5f;
+  err = __fdividef(lim, g3) * (1.0f + kRel) + kRel * fabsf(val);
+  return true;
 }
 
 // Caps of one mesh seen from q, warp-uniform walk: a subtree every lane can take as its far field
@@ -180,7 +212,8 @@ __device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, float
         mom = leaf_moment(M.cap_trec + refs[k], cnts[k]);
       }
       float val = 0.0f, err = 0.0f;
-      const bool far = far_field<float>(qx, qy, qz, n0, n1, n2, k, mom, tau, val, err);
+      const bool far = kFastFarField ? far_field_fast(qx, qy, qz, n0, n1, n2, k, mom, tau, val, err)
+                                     : far_field<float>(qx, qy, qz, n0, n1, n2, k, mom, tau, val, err);
       const bool need = active && !far;
       if (!__any_sync(kFull, need)) {
         if (active) {
@@ -271,10 +304,13 @@ __device__ __forceinline__ void cell_of(const BatchDev &B, uint64_t gcell, int &
   vz = static_cast<int>(cell / (uint64_t(g.nx) * g.ny));
 }
 
-// Pass 2: FP64, one refine cell per lane; a persistent grid that reads the list length on the
-// device, so the whole pass needs no host round trip.
-__global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a) {
-  const unsigned long long n = *a.refine_count;
+// Pass 2: FP64, one listed cell per lane; a persistent grid that reads the list length on the
+// device, so the whole pass needs no host round trip. Cells of `in` that the walk with subtree
+// bound `tau` leaves undecided are appended to `out`.
+__global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a, const uint64_t *__restrict__ in,
+                                                    const unsigned long long *in_count, float tau, uint64_t *out,
+                                                    unsigned long long *out_count) {
+  const unsigned long long n = *in_count;
   const int lane = threadIdx.x & 31;
   const BatchDev &B = a.batch;
   bool corrupt = false;
@@ -285,7 +321,7 @@ __global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a) {
     const bool active = k < n;
     int mesh, vx, vy, vz;
     uint64_t cell;
-    cell_of(B, active ? a.refine[k] : a.refine[base], mesh, vx, vy, vz, cell);
+    cell_of(B, active ? in[k] : in[base], mesh, vx, vy, vz, cell);
     const MeshRec &M = B.recs[mesh];
     const GridDev g = M.g;
     const float fz = cell_center(g.oz, vz, g.voxel);
@@ -295,7 +331,7 @@ __global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a) {
     const int first_mesh = __shfl_sync(kFull, mesh, 0);
     const bool uniform = __all_sync(kFull, mesh == first_mesh);
     if (uniform) {
-      if (M.cap_root >= 0) caps_walk<double, true>(a, M, active, qx, qy, qz, kTau64, wex, eps, corrupt);
+      if (M.cap_root >= 0) caps_walk<double, true>(a, M, active, qx, qy, qz, tau, wex, eps, corrupt);
     } else {
       unsigned pending = __ballot_sync(kFull, true);
       while (pending) {
@@ -304,7 +340,7 @@ __global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a) {
         const bool mine = mesh == mm;
         const MeshRec &MM = B.recs[mm];
         if (MM.cap_root >= 0)
-          caps_walk<double, true>(a, MM, active && mine, qx, qy, qz, kTau64, wex, eps, corrupt);
+          caps_walk<double, true>(a, MM, active && mine, qx, qy, qz, tau, wex, eps, corrupt);
         pending &= ~__ballot_sync(kFull, mine);
       }
     }
@@ -315,8 +351,8 @@ __global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a) {
     if (c - e > 0.5) {
       M.dist[cell] = -fabsf(M.dist[cell]);
     } else if (!(c + e < 0.5)) {
-      const unsigned long long at = atomicAdd(a.direct_count, 1ull);
-      a.direct[at] = a.refine[k];
+      const unsigned long long at = atomicAdd(out_count, 1ull);
+      out[at] = in[k];
     }
   }
   if (corrupt) atomic_or_err(a.err, kErrCorruptTree);
@@ -326,11 +362,11 @@ __global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a) {
 __global__ __launch_bounds__(kThreads) void k_gwn_direct(GwnArgs a) {
   __shared__ double part[kThreads / kWarp];
   const BatchDev &B = a.batch;
-  const unsigned long long n = *a.direct_count;
+  const unsigned long long n = *a.final_count;
   for (unsigned long long k = blockIdx.x; k < n; k += gridDim.x) {
     int mesh, vx, vy, vz;
     uint64_t cell;
-    cell_of(B, a.direct[k], mesh, vx, vy, vz, cell);
+    cell_of(B, a.refine[k], mesh, vx, vy, vz, cell);
     const MeshRec &M = B.recs[mesh];
     const GridDev g = M.g;
     const float fz = cell_center(g.oz, vz, g.voxel);
@@ -369,7 +405,8 @@ cudaError_t gwn_enqueue(const GwnInput &in, void *temp, int num_sms, cudaStream_
   if (B.total_gwn_tiles == 0) return cudaSuccess;
   const size_t list_bytes = (in.gwn_cells * 8 + 255) & ~size_t(255);
   char *base = static_cast<char *>(temp);
-  unsigned long long *counters = reinterpret_cast<unsigned long long *>(base);  // [0] tiles [1] refine [2] direct
+  // [0] tiles, [1] pass 1's list, [2] coarse pass 2's, [3] fine pass 2's (the direct sum's cells)
+  unsigned long long *counters = reinterpret_cast<unsigned long long *>(base);
   GwnArgs a;
   a.batch = B;
   a.col_start = in.col_start;
@@ -380,6 +417,7 @@ cudaError_t gwn_enqueue(const GwnInput &in, void *temp, int num_sms, cudaStream_
   a.refine_count = counters + 1;
   a.direct = reinterpret_cast<uint64_t *>(base + 256 + list_bytes);
   a.direct_count = counters + 2;
+  a.final_count = counters + 3;
   a.tile_counter = counters;
   a.err = in.err;
   cudaError_t e = cudaMemsetAsync(counters, 0, 64, st);
@@ -393,7 +431,12 @@ cudaError_t gwn_enqueue(const GwnInput &in, void *temp, int num_sms, cudaStream_
   blocks = std::min<long long>(blocks, static_cast<long long>((B.total_gwn_tiles + 7) / 8));
   k_gwn32<<<static_cast<unsigned>(std::max<long long>(blocks, 1)), kThreads, 0, st>>>(a);
   note_launch();
-  k_gwn64<<<static_cast<unsigned>(num_sms * 8), kThreads, 0, st>>>(a);
+  k_gwn64<<<static_cast<unsigned>(num_sms * 8), kThreads, 0, st>>>(a, a.refine, a.refine_count, kTau64, a.direct,
+                                                                   a.direct_count);
+  note_launch();
+  // the refine list has been read by now (stream order): it receives the fine pass's leftovers
+  k_gwn64<<<static_cast<unsigned>(num_sms * 8), kThreads, 0, st>>>(a, a.direct, a.direct_count, kTau64Fine,
+                                                                   a.refine, a.final_count);
   note_launch();
   k_gwn_direct<<<static_cast<unsigned>(num_sms * 4), kThreads, 0, st>>>(a);
   note_launch();
@@ -402,4 +445,4 @@ cudaError_t gwn_enqueue(const GwnInput &in, void *temp, int num_sms, cudaStream_
 
 uint64_t *gwn_refine_counter(void *temp) { return reinterpret_cast<uint64_t *>(static_cast<char *>(temp)) + 1; }
 
-uint64_t *gwn_direct_counter(void *temp) { return reinterpret_cast<uint64_t *>(static_cast<char *>(temp)) + 2; }
+uint64_t *gwn_direct_counter(void *temp) { return reinterpret_cast<uint64_t *>(static_cast<char *>(temp)) + 3; }

@@ -122,10 +122,7 @@ __global__ __launch_bounds__(kThreads) void k_prep(BatchDev B, TriRec *__restric
       r.r0 = make_float4(a.x, a.y, a.z, inv_or_zero(e1x * e1x + e1y * e1y + e1z * e1z));
       r.r1 = make_float4(e1x, e1y, e1z, inv_or_zero(e2x * e2x + e2y * e2y + e2z * e2z));
       r.r2 = make_float4(e2x, e2y, e2z, inv_or_zero(e3x * e3x + e3y * e3y + e3z * e3z));
-      const float n2 = nx * nx + ny * ny + nz * nz;
-      // The normal counts only when it is well above rounding noise.
-      const float scale = fmaxf(e1x * e1x + e1y * e1y + e1z * e1z, e2x * e2x + e2y * e2y + e2z * e2z);
-      r.r3 = make_float4(nx, ny, nz, (n2 > 1e-12f * scale * scale) ? 1.0f / n2 : 0.0f);
+      r.r3 = make_float4(nx, ny, nz, sqrtf(nx * nx + ny * ny + nz * nz));
       rec[t] = r;
     }
     const float4 l = make_float4(fminf(fminf(a.x, b.x), c.x), fminf(fminf(a.y, b.y), c.y),
@@ -411,10 +408,9 @@ __global__ __launch_bounds__(kThreads) void k_gather(BatchDev B, const uint32_t 
 
 // Far-field moments of every inner node, bottom-up like k_refit: (sum of a_i n_i, sum of a_i)
 // over its triangles, a_i the area and n_i the unit normal. A triangle's a_i n_i is half its edge
-// cross product, the r3 of its record.
+// cross product, the r3 of its record (whose w is the product's length).
 __device__ __forceinline__ float4 tri_moment(const TriRec &t) {
-  return make_float4(0.5f * t.r3.x, 0.5f * t.r3.y, 0.5f * t.r3.z,
-                     0.5f * sqrtf(t.r3.x * t.r3.x + t.r3.y * t.r3.y + t.r3.z * t.r3.z));
+  return make_float4(0.5f * t.r3.x, 0.5f * t.r3.y, 0.5f * t.r3.z, 0.5f * t.r3.w);
 }
 
 __global__ __launch_bounds__(kThreads) void k_moments(int n, const TriRec *__restrict__ tris,
