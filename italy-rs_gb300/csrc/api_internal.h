@@ -213,6 +213,9 @@ cudaError_t caps_device(const float *verts, uint32_t V, const uint32_t *idx, uin
 // every_gwn: also the winding-number meshes without a distance output (resident meshes).
 sdfb_status device_caps(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &ms, bool every_gwn = false);
 
+// Winding-number pass 1 tiles: 4 x 4 x (2 kGwnCellsPerLane) cells, kGwnCellsPerLane per lane.
+constexpr int kGwnCellsPerLane = 4;
+constexpr int kGwnTileZ = 2 * kGwnCellsPerLane;
 // gwn.cu: flips the sign of cells whose generalized winding number says inside (enqueued only).
 size_t gwn_temp_bytes(uint64_t gwn_cells);
 cudaError_t gwn_enqueue(const GwnInput &in, void *temp, int num_sms, cudaStream_t st);

@@ -94,6 +94,22 @@ __device__ __forceinline__ int column_winding(const GwnArgs &a, const MeshRec &M
   return w;
 }
 
+// The same for V heights of one column, reading its crossings once.
+template <int V>
+__device__ __forceinline__ void column_windings(const GwnArgs &a, const MeshRec &M, int vx, int vy,
+                                                const float (&pz)[V], int (&w)[V]) {
+  const uint64_t col = M.col_base + uint64_t(vy) * M.g.nx + vx;
+  const uint64_t s0 = __ldg(a.col_start + col), s1 = __ldg(a.col_start + col + 1);
+#pragma unroll
+  for (int v = 0; v < V; ++v) w[v] = 0;
+  for (uint64_t k = s0; k < s1; ++k) {
+    const float z = __ldg(a.col_z + k);
+    const int s = __ldg(a.col_s + k);
+#pragma unroll
+    for (int v = 0; v < V; ++v) w[v] += z > pz[v] ? s : 0;
+  }
+}
+
 // The far field of a cap cluster -- moment m = (D, A), inside the child box of centre c and half
 // extent e (so inside the ball of radius |e| about c) -- seen from q: false when q is too close
 // (r <= 2 |e|) or the error bound exceeds tau; else val = D . (c - q) / r^3 and err bounds
@@ -160,10 +176,11 @@ __device__ __forceinline__ bool far_field_fast(float qx, float qy, float qz, con
 // descends, and leaves give exact solid angles. T is the accumulation type. The far field is
 // evaluated in FP32 either way (its error bound carries FP32's rounding); with EXACT64 the leaves'
 // exact solid angles are FP64, from the original cap vertices, and everything is summed in FP64.
-// q is a cell centre, an FP32 value.
-template <typename T, bool EXACT64>
-__device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, float qx, float qy, float qz, float tau,
-                          T &wex, T &eps, bool &corrupt) {
+// q is a cell centre, an FP32 value; a lane walks for V cells of one column (heights qz[v]), and
+// a subtree is taken as a far field only when it is one for every cell of the warp.
+template <typename T, bool EXACT64, int V>
+__device__ void caps_walk(const GwnArgs &a, const MeshRec &M, const bool (&active)[V], float qx, float qy,
+                          const float (&qz)[V], float tau, T (&wex)[V], T (&eps)[V], bool &corrupt) {
   const int lane = threadIdx.x & 31;
   int cur = M.cap_root, sp = 0, stk0 = 0, stk1 = 0;
   const long long step_limit = 2ll * M.cap_nodes_n + 64;
@@ -211,15 +228,23 @@ __device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, float
         }
         mom = leaf_moment(M.cap_trec + refs[k], cnts[k]);
       }
-      float val = 0.0f, err = 0.0f;
-      const bool far = kFastFarField ? far_field_fast(qx, qy, qz, n0, n1, n2, k, mom, tau, val, err)
-                                     : far_field<float>(qx, qy, qz, n0, n1, n2, k, mom, tau, val, err);
-      const bool need = active && !far;
+      float val[V], err[V];
+      bool need = false;
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        val[v] = 0.0f;
+        err[v] = 0.0f;
+        const bool far = kFastFarField ? far_field_fast(qx, qy, qz[v], n0, n1, n2, k, mom, tau, val[v], err[v])
+                                       : far_field<float>(qx, qy, qz[v], n0, n1, n2, k, mom, tau, val[v], err[v]);
+        need |= active[v] && !far;
+      }
       if (!__any_sync(kFull, need)) {
-        if (active) {
-          wex += T(val);
-          eps += T(err);
-        }
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+          if (active[v]) {
+            wex[v] += T(val[v]);
+            eps[v] += T(err[v]);
+          }
         continue;
       }
       if (cnts[k] == 0) {
@@ -230,20 +255,30 @@ __device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, float
       for (int j = 0; j < cnts[k]; ++j) {
         if (EXACT64) {
           const uint32_t t = __ldg(M.cap_order + refs[k] + j);
-          V3<T> p[3];
+          float c3[3][3];
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             const uint32_t i = __ldg(M.cidx + 3ull * t + c);
-            p[c] = {T(__ldg(M.cverts + 3ull * i)) - qx, T(__ldg(M.cverts + 3ull * i + 1)) - qy,
-                    T(__ldg(M.cverts + 3ull * i + 2)) - qz};
+            c3[c][0] = __ldg(M.cverts + 3ull * i);
+            c3[c][1] = __ldg(M.cverts + 3ull * i + 1);
+            c3[c][2] = __ldg(M.cverts + 3ull * i + 2);
           }
-          wex += solid_angle<T>(p[0], p[1], p[2]);
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            V3<T> p[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) p[c] = {T(c3[c][0]) - T(qx), T(c3[c][1]) - T(qy), T(c3[c][2]) - T(qz[v])};
+            wex[v] += solid_angle<T>(p[0], p[1], p[2]);
+          }
         } else {
           const TriRec *tr = M.cap_trec + refs[k] + j;
           const float4 r0 = __ldg(&tr->r0), r1 = __ldg(&tr->r1), r2 = __ldg(&tr->r2);
-          const V3<T> p{T(r0.x) - qx, T(r0.y) - qy, T(r0.z) - qz};
-          wex += solid_angle<T>(p, {p.x + T(r1.x), p.y + T(r1.y), p.z + T(r1.z)},
-                                {p.x + T(r2.x), p.y + T(r2.y), p.z + T(r2.z)});
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            const V3<T> p{T(r0.x) - T(qx), T(r0.y) - T(qy), T(r0.z) - T(qz[v])};
+            wex[v] += solid_angle<T>(p, {p.x + T(r1.x), p.y + T(r1.y), p.z + T(r1.z)},
+                                     {p.x + T(r2.x), p.y + T(r2.y), p.z + T(r2.z)});
+          }
         }
       }
     }
@@ -251,9 +286,10 @@ __device__ void caps_walk(const GwnArgs &a, const MeshRec &M, bool active, float
   }
 }
 
-// Pass 1: FP32 over warp tiles of 4 x 4 x 2 cells of the winding-number meshes.
+// Pass 1: FP32 over warp tiles of 4 x 4 x kGwnTileZ cells of the winding-number meshes, each lane
+// walking for kGwnCellsPerLane cells of one column (the node loads, votes and stack are shared).
 __global__ __launch_bounds__(kThreads) void k_gwn32(GwnArgs a) {
-  constexpr int TX = 4, TY = 4, TZ = 2;
+  constexpr int TX = 4, TY = 4, TZ = kGwnTileZ, V = kGwnCellsPerLane;
   const int lane = threadIdx.x & 31;
   const int lx = lane % TX, ly = (lane / TX) % TY, lz = lane / (TX * TY);
   const BatchDev &B = a.batch;
@@ -271,24 +307,39 @@ __global__ __launch_bounds__(kThreads) void k_gwn32(GwnArgs a) {
     const int tx = static_cast<int>(local % tiles_x);
     const unsigned long long rest = local / tiles_x;
     const int ty = static_cast<int>(rest % tiles_y), tz = static_cast<int>(rest / tiles_y);
-    const int vx = tx * TX + lx, vy = ty * TY + ly, vz = tz * TZ + lz;
-    const bool active = vx < g.nx && vy < g.ny && vz < g.nz;
-    const float qx = cell_center(g.ox, vx, g.voxel), qy = cell_center(g.oy, vy, g.voxel),
-                qz = cell_center(g.oz, vz, g.voxel);
-    float wex = 0.0f, eps = 0.0f;
-    if (M.cap_root >= 0) caps_walk<float, false>(a, M, active, qx, qy, qz, kTau32, wex, eps, corrupt);
-    if (!active) continue;
-    const int W = column_winding(a, M, vx, vy, qz);
-    const uint64_t cell = (uint64_t(vz) * g.ny + vy) * g.nx + vx;
-    const float d = M.dist[cell];
-    const float c = fabsf(float(W) - wex * float(kInv4Pi));
-    const float e = eps * float(kInv4Pi) + 1e-5f * (1.0f + fabsf(wex));
-    const bool band = d <= a.band_voxels * g.voxel;
-    if (!band && c - e > 0.5f) {
-      M.dist[cell] = -d;
-    } else if (band || !(c + e < 0.5f)) {
-      const unsigned long long at = atomicAdd(a.refine_count, 1ull);
-      a.refine[at] = B.cell_starts[mesh] + cell;
+    const int vx = tx * TX + lx, vy = ty * TY + ly;
+    bool active[V];
+    float qz[V], wex[V], eps[V];
+    bool any_active = false;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const int vz = tz * TZ + lz + 2 * v;
+      active[v] = vx < g.nx && vy < g.ny && vz < g.nz;
+      any_active |= active[v];
+      qz[v] = cell_center(g.oz, vz, g.voxel);
+      wex[v] = 0.0f;
+      eps[v] = 0.0f;
+    }
+    const float qx = cell_center(g.ox, vx, g.voxel), qy = cell_center(g.oy, vy, g.voxel);
+    if (M.cap_root >= 0) caps_walk<float, false, V>(a, M, active, qx, qy, qz, kTau32, wex, eps, corrupt);
+    if (!any_active) continue;
+    int W[V];
+    column_windings<V>(a, M, vx, vy, qz, W);
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      if (!active[v]) continue;
+      const int vz = tz * TZ + lz + 2 * v;
+      const uint64_t cell = (uint64_t(vz) * g.ny + vy) * g.nx + vx;
+      const float d = M.dist[cell];
+      const float c = fabsf(float(W[v]) - wex[v] * float(kInv4Pi));
+      const float e = eps[v] * float(kInv4Pi) + 1e-5f * (1.0f + fabsf(wex[v]));
+      const bool band = d <= a.band_voxels * g.voxel;
+      if (!band && c - e > 0.5f) {
+        M.dist[cell] = -d;
+      } else if (band || !(c + e < 0.5f)) {
+        const unsigned long long at = atomicAdd(a.refine_count, 1ull);
+        a.refine[at] = B.cell_starts[mesh] + cell;
+      }
     }
   }
   if (corrupt) atomic_or_err(a.err, kErrCorruptTree);
@@ -326,12 +377,14 @@ __global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a, const uint64_t *_
     const GridDev g = M.g;
     const float fz = cell_center(g.oz, vz, g.voxel);
     const double qx = cell_center(g.ox, vx, g.voxel), qy = cell_center(g.oy, vy, g.voxel), qz = fz;
-    double wex = 0.0, eps = 0.0;
+    double wex[1] = {0.0}, eps[1] = {0.0};
+    const float qzs[1] = {fz};
     // lanes of one warp may belong to different meshes: walk each distinct mesh in turn
     const int first_mesh = __shfl_sync(kFull, mesh, 0);
     const bool uniform = __all_sync(kFull, mesh == first_mesh);
     if (uniform) {
-      if (M.cap_root >= 0) caps_walk<double, true>(a, M, active, qx, qy, qz, tau, wex, eps, corrupt);
+      const bool act[1] = {active};
+      if (M.cap_root >= 0) caps_walk<double, true, 1>(a, M, act, float(qx), float(qy), qzs, tau, wex, eps, corrupt);
     } else {
       unsigned pending = __ballot_sync(kFull, true);
       while (pending) {
@@ -339,15 +392,16 @@ __global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a, const uint64_t *_
         const int mm = __shfl_sync(kFull, mesh, leader);
         const bool mine = mesh == mm;
         const MeshRec &MM = B.recs[mm];
+        const bool act[1] = {active && mine};
         if (MM.cap_root >= 0)
-          caps_walk<double, true>(a, MM, active && mine, qx, qy, qz, tau, wex, eps, corrupt);
+            caps_walk<double, true, 1>(a, MM, act, float(qx), float(qy), qzs, tau, wex, eps, corrupt);
         pending &= ~__ballot_sync(kFull, mine);
       }
     }
     if (!active) continue;
     const int W = column_winding(a, M, vx, vy, fz);
-    const double c = fabs(double(W) - wex * kInv4Pi);
-    const double e = eps * kInv4Pi + 1e-12 * (1.0 + fabs(wex));
+    const double c = fabs(double(W) - wex[0] * kInv4Pi);
+    const double e = eps[0] * kInv4Pi + 1e-12 * (1.0 + fabs(wex[0]));
     if (c - e > 0.5) {
       M.dist[cell] = -fabsf(M.dist[cell]);
     } else if (!(c + e < 0.5)) {

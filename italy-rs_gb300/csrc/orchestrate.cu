@@ -230,7 +230,7 @@ void make_layout(sdfb_ctx *ctx, const std::vector<PlanMesh> &ms, const sdfb_opts
     L.tile[m + 1] = L.tile[m] + (p.dist ? tiles_for(r.g, L.tile_id) : 0);
     const bool gwn = p.dist && r.sign == kSignGwn;
     L.gtile[m + 1] = L.gtile[m] + (gwn ? uint64_t((p.grid.nx + 3) / 4) * uint64_t((p.grid.ny + 3) / 4) *
-                                             uint64_t((p.grid.nz + 1) / 2)
+                                             uint64_t((p.grid.nz + kGwnTileZ - 1) / kGwnTileZ)
                                        : 0);
     if (gwn) {
       L.gwn_cells += cells;
