@@ -2,7 +2,7 @@
 """Benchmark of the GB300 mesh -> SDF bake.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload batch64|c1|c2|c3] [--serve-seconds S] [--no-serve] [--no-configs]
+                    [--workload batch64|c1|c2|c3|sparse] [--serve-seconds S] [--no-serve] [--no-configs]
 
 Workloads (seeded synthetic meshes generated in-process; no dataset is involved):
 
@@ -19,6 +19,9 @@ Workloads (seeded synthetic meshes generated in-process; no dataset is involved)
 * ``c3``: the 500k-triangle soup (displaced spheres and tori, 2% of faces deleted) on a 512^3 grid,
   FP32 distance, winding-number sign with FP64 inside the one-voxel band.
   For c1-c3 a step is one single-mesh bake (through the batch entry point, a batch of one).
+* ``sparse``: a side workload for the sparse voxelizer (voxelizeMesh's cell list): the 1M-triangle
+  displaced torus at resolution 512 through sdfb_voxelize_sparse, grid cells/s (a short line of
+  its own, without the headline's keys).
 
 The default line also carries ``configs``: for c1, c2 and c3 the single-mesh GPU bake time and
 voxels/s (device buffers, and end to end from host buffers), max and RMS distance error over the
@@ -73,7 +76,7 @@ def parse(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="batch64", choices=["batch64", "c1", "c2", "c3", "displaced-sphere-256"])
+    ap.add_argument("--workload", default="batch64", choices=["batch64", "c1", "c2", "c3", "displaced-sphere-256", "sparse"])
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -771,11 +774,52 @@ def batch_classes(sdfb, ctx, torch, stream, flush, devm, grids, dptr, optr, opts
     return out
 
 
+def sparse_main(args):
+    """voxelizeMesh's sparse cell list (sdfb_voxelize_sparse) of the 1M-triangle displaced torus at
+    resolution 512 (134 M grid cells): occupancy, per-tile compaction and the insertion-order sort,
+    timed end to end through the host entry point (soup up, cell list down), median of the steps.
+    A side workload for the compaction kernels, not the headline line."""
+    import numpy as np
+    import torch
+
+    import sdfb
+    from sdfb import meshgen as mg
+
+    ctx = sdfb.Context(0)
+    v, f = mg.displaced_torus(1024, 512, 0.3, 0.1, 1114)
+    soup = np.ascontiguousarray(np.asarray(v, np.float32)[np.asarray(f, np.int64)].reshape(-1, 3))
+    bmin, bmax = soup.min(0), soup.max(0)
+    res = 512
+    stage(f"sparse: {len(f)} triangles, resolution {res}")
+    for _ in range(max(args.warmup, 1)):
+        cells, _, _ = ctx.voxelize_sparse(soup, bmin, bmax, res)
+    times = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cells, _, _ = ctx.voxelize_sparse(soup, bmin, bmax, res)
+        times.append(time.perf_counter() - t0)
+    times.sort()
+    t = times[len(times) // 2]
+    print(json.dumps({"metric": "sparse voxelize (voxelizeMesh cell list) grid cells/s", "value": res ** 3 / t,
+                      "unit": "cells/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": 1e3 * t, "higher_is_better": True, "dtype": "u8",
+                      "data": "synthetic (seeded mesh generated in-process)",
+                      "config": {"workload": "sparse", "triangles": int(len(f)), "resolution": res,
+                                 "cells_listed": int(len(cells)),
+                                 "timing": "host wall clock around sdfb_voxelize_sparse (copies included)"}}),
+          flush=True)
+    ctx.close()
+
+
 def main(argv=None):
     args = parse(argv)
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "sparse":
+        sparse_main(args)
         return
     import numpy as np
     import torch

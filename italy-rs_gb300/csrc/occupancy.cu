@@ -75,11 +75,22 @@ __global__ __launch_bounds__(kThreads) void k_occ_items(BatchDev B, uint64_t *__
   items[t] = uint64_t(tc.hi[0] - tc.lo[0] + 1) * uint64_t(tc.hi[1] - tc.lo[1] + 1) * uint64_t(tc.hi[2] - tc.lo[2] + 1);
 }
 
-// Clears the occupancy grids of the batch (one pass over the global cells).
+// Clears the occupancy grids of the batch (one pass over the global cells). A thread clears 16
+// consecutive cells, with one 16-byte store where they lie in one mesh's grid at an aligned
+// address (so a warp writes 512 contiguous bytes), else byte by byte.
 __global__ __launch_bounds__(kThreads) void k_occ_clear(BatchDev B) {
   const uint64_t stride = uint64_t(gridDim.x) * kThreads * 16;
   for (uint64_t c0 = (uint64_t(blockIdx.x) * kThreads + threadIdx.x) * 16; c0 < B.total_cells; c0 += stride) {
     int m = find_mesh(B.cell_starts, B.num_meshes, c0);
+    if (c0 + 16 <= B.cell_starts[m + 1]) {
+      uint8_t *occ = B.recs[m].occ;
+      if (!occ) continue;
+      uint8_t *p = occ + (c0 - B.cell_starts[m]);
+      if ((reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+        *reinterpret_cast<uint4 *>(p) = make_uint4(0u, 0u, 0u, 0u);
+        continue;
+      }
+    }
     for (uint64_t c = c0; c < c0 + 16 && c < B.total_cells; ++c) {
       while (c >= B.cell_starts[m + 1]) ++m;
       uint8_t *occ = B.recs[m].occ;

@@ -22,22 +22,24 @@ def holey_soup(seed: int, sphere_level=3, torus=(48, 16), fraction=0.05):
     return mg.delete_faces(v, f, fraction, int(rng.integers(1 << 30)))
 
 
-@pytest.mark.parametrize("seed,n", [(3, 40), (4, 56)])
-def test_gwn_sign_matches_fp64_oracle(ctx, oracle, seed, n):
+@pytest.mark.parametrize("seed,n,dims", [(3, 40, None), (4, 56, None), (5, 44, (37, 41, 29))])
+def test_gwn_sign_matches_fp64_oracle(ctx, oracle, seed, n, dims):
+    """dims: a grid whose edges are not multiples of the winding-number tile (4 x 4 x 8 cells)."""
     import sdfb
     v, f = holey_soup(seed)
     origin, voxel = (-0.5,) * 3, 1.0 / n
-    grid = sdfb.make_grid(origin, voxel, (n, n, n))
+    dims = dims or (n, n, n)
+    grid = sdfb.make_grid(origin, voxel, dims)
     st = sdfb.Stats()
     st.struct_size = sdfb.C.sizeof(sdfb.Stats)
     dist, occ = ctx.bake(v, f, grid, sdfb.make_opts(sign_mode=sdfb.SIGN_AUTO), stats=st)
     assert st.watertight == 0 and st.sign_mode_used == sdfb.SIGN_GWN
     assert st.gwn_fp64_cells > 0
     flat = dist.reshape(-1)
-    d64 = oracle.distance(v, f, origin, voxel, (n, n, n))
+    d64 = oracle.distance(v, f, origin, voxel, dims)
     assert np.abs(np.abs(flat.astype(np.float64)) - d64).max() <= DIST_TOL * np.sqrt(3)
-    assert np.array_equal(occ.reshape(-1), oracle.occupancy(v, f, origin, voxel, (n, n, n)))
-    w = oracle.gwn(v, f, origin, voxel, (n, n, n))
+    assert np.array_equal(occ.reshape(-1), oracle.occupancy(v, f, origin, voxel, dims))
+    w = oracle.gwn(v, f, origin, voxel, dims)
     far = (d64 > voxel) & (np.abs(np.abs(w) - 0.5) > 1e-6)
     bad = np.count_nonzero((flat[far] < 0) != (np.abs(w[far]) > 0.5))
     assert bad == 0, f"{bad} winding-number sign mismatches outside the band"
