@@ -19,9 +19,10 @@
 // the summed bounds cannot move |w| across 0.5.
 //
 // Precision split:
-//   pass 1 (FP32, every cell of every winding-number mesh, warp tiles of 4 x 4 x 2): cells
-//     outside the band (|d| > band_voxels * voxel) whose interval [c - e, c + e] lies on one side
-//     of |w| = 0.5 get their sign; the band and undecided cells go to a refine list.
+//   pass 1 (FP32, every cell of every winding-number mesh, warp tiles of 4 x 4 x 8, four cells
+//     of a column per lane): cells outside the band (|d| > band_voxels * voxel) whose interval
+//     [c - e, c + e] lies on one side of |w| = 0.5 get their sign; the band and undecided cells
+//     go to a refine list.
 //   pass 2 (FP64 accumulation, exact cap solid angles in FP64 from the original FP32 vertices,
 //     the same FP32 far field): signs of the refine list, first with coarse subtrees (kTau64),
 //     then the cells that stay undecided again with fine ones (kTau64Fine); a cell still
