@@ -188,3 +188,53 @@ def test_close_with_requests_queued(ctx):
     t.start()
     t.join(60)
     assert not t.is_alive()
+
+
+def test_registration_while_waves_run(ctx):
+    """New meshes registered while another thread keeps waves in flight (waves launched during a
+    registration leave SMs free and run one after another): every result of the resident mesh is
+    bit-identical to it alone, and each new mesh's result matches its plain bake."""
+    import threading
+
+    import sdfb
+    from sdfb import meshgen as mg
+    base = mg.displaced_torus(64, 24, 0.27, 0.1, 21)
+    news = [mg.displaced_icosphere(4, 0.28, 30 + k) for k in range(4)]
+    n = 48
+    g = sdfb.make_grid((-0.5,) * 3, 1.0 / n, (n, n, n))
+    with sdfb.Server(ctx) as srv:
+        mid = srv.register(*base)
+        d0 = np.empty(g.shape, np.float32)
+        o0 = np.empty(g.shape, np.uint8)
+        assert srv.poll(srv.submit(mid, g, d0, o0), 60000)[0]
+        outs, errors, stop = [], [], threading.Event()
+
+        def busy():
+            try:
+                while not stop.is_set():
+                    d = np.empty(g.shape, np.float32)
+                    o = np.empty(g.shape, np.uint8)
+                    done, info = srv.poll(srv.submit(mid, g, d, o), 60000)
+                    assert done and info["status"] == 0
+                    outs.append((d, o))
+            except Exception as e:  # reported on the main thread
+                errors.append(e)
+
+        th = [threading.Thread(target=busy) for _ in range(3)]
+        [t.start() for t in th]
+        results = []
+        for v, f in news:
+            nid = srv.register(v, f)
+            d = np.empty(g.shape, np.float32)
+            o = np.empty(g.shape, np.uint8)
+            assert srv.poll(srv.submit(nid, g, d, o), 60000)[0]
+            results.append((v, f, d, o))
+        stop.set()
+        [t.join() for t in th]
+        assert not errors, errors
+        assert outs
+        for d, o in outs:
+            assert np.array_equal(d, d0) and np.array_equal(o, o0)
+    for v, f, d, o in results:
+        d1, o1 = ctx.bake(v, f, g, sdfb.make_opts())
+        assert_same_bake(d, o, d1, o1)
