@@ -15,8 +15,9 @@
 //     wave while a wave slot is free and the budget holds (resident meshes + every in-flight
 //     wave's outputs). A wave is one batched launch sequence (orchestrate.cu) over all its
 //     requests; waves run on separate streams, so a wave admitted while others are on the GPU
-//     overlaps with them. Each cell is computed exactly as in a single bake, so a result is the
-//     same alone and in any mix.
+//     overlaps with them. Each cell is computed as in a single bake with the wave's launch
+//     parameters (those of its largest grid), so a result is the same alone and in any mix up to
+//     rounding where two triangles nearly tie (bit for bit under the same parameters).
 //   * Outputs go straight to the caller's buffers when they are pinned (a pinned distance grid is
 //     written in place by the distance kernel, occupancy by cudaMemcpyAsync), else through the
 //     wave's pinned staging buffer and a host copy when the wave retires.

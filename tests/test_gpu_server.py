@@ -1,8 +1,10 @@
-"""Serving loop: continuous batching over resident meshes. A served result is bit-identical
-whatever else shares its wave (each cell is computed the same way on the mesh's resident
-hierarchy), and equals the same bake run alone through the plain entry point up to rounding: the
-resident hierarchy is built with the leaf size tuned for a 256^3 grid, the plain bake tunes for its
-own grid, and where two triangles nearly tie with an FP32 box bound the walks may keep either."""
+"""Serving loop: continuous batching over resident meshes. A served result equals the same
+request alone, and the same bake run through the plain entry point, within the tolerance: occupancy
+and signs identical, distances up to rounding (4e-7). A wave takes its launch parameters (tile
+shape, stack depth, deferral budget) from its largest grid, the resident hierarchy is built with
+the leaf size tuned for a 256^3 grid while a plain bake tunes for its own grid, and where two
+triangles nearly tie with an FP32 box bound, walks in a different order may keep either. With the
+same launch parameters the served result is bit-identical to the request alone."""
 from __future__ import annotations
 
 import numpy as np
@@ -47,7 +49,7 @@ def test_served_equals_plain_in_the_mix(ctx):
             done, info = srv.poll(rid, 60000)
             assert done and info["status"] == 0
             infos.append(info)
-            if k < 3:  # the same request in a mixed wave: bit-identical to it alone
+            if k < 3:  # the same request in a mixed wave (here with its lone launch parameters)
                 assert np.array_equal(d, alone[k][0]) and np.array_equal(o, alone[k][1])
             d1, o1 = ctx.bake(*meshes[m], g, sdfb.make_opts())
             assert_same_bake(d, o, d1, o1)
@@ -191,9 +193,10 @@ def test_close_with_requests_queued(ctx):
 
 
 def test_registration_while_waves_run(ctx):
-    """New meshes registered while another thread keeps waves in flight (waves launched during a
-    registration leave SMs free and run one after another): every result of the resident mesh is
-    bit-identical to it alone, and each new mesh's result matches its plain bake."""
+    """New meshes registered while other threads keep waves in flight (waves launched during a
+    registration leave SMs free and run one after another; a wave holding a new mesh may take other
+    launch parameters): every result of the resident mesh matches it alone within the tolerance,
+    and each new mesh's result matches its plain bake."""
     import threading
 
     import sdfb
@@ -234,7 +237,7 @@ def test_registration_while_waves_run(ctx):
         assert not errors, errors
         assert outs
         for d, o in outs:
-            assert np.array_equal(d, d0) and np.array_equal(o, o0)
+            assert_same_bake(d, o, d0, o0)
     for v, f, d, o in results:
         d1, o1 = ctx.bake(v, f, g, sdfb.make_opts())
         assert_same_bake(d, o, d1, o1)
