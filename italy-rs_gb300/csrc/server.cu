@@ -44,12 +44,14 @@ using namespace sdfb;
 namespace {
 
 constexpr int kRegSlots = 4;  // meshes registered (uploaded, gated, built) at the same time
-// While a registration is in progress, waves launch their persistent kernels on kReserveSms fewer
-// SMs and each wave's work waits for the previous wave's (kSerialWaves): a wave's persistent
-// distance kernel otherwise holds every SM until it ends, and each step of a registration (gate,
-// caps, hierarchy, separated by host reads) would wait for the waves queued ahead of it.
-constexpr int kReserveSms = 8;
-constexpr bool kSerialWaves = true;
+// While a registration is in progress, waves may launch their persistent kernels on kReserveSms
+// fewer SMs and run one after another (kSerialWaves), so that a registration's steps (gate, caps,
+// hierarchy, separated by host reads) are not queued behind the waves in flight. Off: on the
+// serving stream (Poisson 200 requests/s, 70% new meshes) 8 reserved SMs with serial waves halved
+// register()'s own latency but lowered capacity 974 -> 933 M voxels/s and doubled the requests'
+// p50 (0.37 -> 0.73-1.9 s); registration streams keep the highest priority instead.
+constexpr int kReserveSms = 0;
+constexpr bool kSerialWaves = false;
 
 double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
