@@ -193,10 +193,10 @@ def test_close_with_requests_queued(ctx):
 
 
 def test_registration_while_waves_run(ctx):
-    """New meshes registered while other threads keep waves in flight (waves launched during a
-    registration leave SMs free and run one after another; a wave holding a new mesh may take other
-    launch parameters): every result of the resident mesh matches it alone within the tolerance,
-    and each new mesh's result matches its plain bake."""
+    """New meshes registered while other threads keep waves in flight (registrations run on
+    high-priority streams beside the waves; a wave holding a new mesh may take other launch
+    parameters): every result of the resident mesh matches it alone within the tolerance, and each
+    new mesh's result matches its plain bake."""
     import threading
 
     import sdfb
