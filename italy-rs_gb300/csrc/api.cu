@@ -197,6 +197,13 @@ sdfb_status device_caps(sdfb_ctx *ctx, cudaStream_t st, std::vector<PlanMesh> &m
       ++ng;
     }
   if (ng == 0) return SDFB_OK;
+  // Cap vertices are numbered V + loop and half-edges are labelled by 32-bit indices.
+  for (const PlanMesh &p : ms)
+    if (p.sign == kSignGwn && (p.dist || every_gwn)) {
+      const uint64_t V = p.pverts ? p.pV : p.V, T = p.pverts ? p.pT : p.T;
+      if (V + 3 * T >= (uint64_t(1) << 32))
+        return ctx_fail(ctx, SDFB_ERR_INVALID_ARGUMENT, "mesh too large for winding-number caps (V + 3T >= 2^32)");
+    }
   ENSURE(ctx->in_caps, nv * 4);
   ENSURE(ctx->in_capidx, np * 4);
   ENSURE(ctx->caps_tmp, caps_temp_bytes(tmax));
