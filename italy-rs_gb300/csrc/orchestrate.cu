@@ -7,9 +7,11 @@
 //
 // CUDA events bracket each stage for the per-stage times in sdfb_stats. After the stream drains,
 // the device error word is read: bad indices and non-finite vertices become SDFB_ERR_BAD_MESH; a
-// crossing list that outgrew its buffer is rebuilt at its exact size. For batches whose stages
-// need no host round trip (no winding-number meshes), the launch sequence is captured into a CUDA
-// graph and replayed while the same batch (same tables, sizes and buffers) comes again.
+// crossing list that outgrew its buffer is rebuilt at its exact size. For the batch entry points
+// the launch sequence is captured into a CUDA graph and replayed while the same batch (same
+// tables, sizes and buffers) comes again; no stage inside it needs a host round trip (the
+// winding-number passes read their list lengths on the device, and the caps of winding-number
+// meshes are built before it, by api.cu's device_caps).
 #include <dlfcn.h>
 
 #include <algorithm>

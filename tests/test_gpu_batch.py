@@ -175,3 +175,25 @@ def test_batch_line_of_the_tuning_table(tmp_path, monkeypatch):
     finally:
         ctx_b.close()
         ctx_p.close()
+
+
+def test_winding_number_batch_replays_its_graph(ctx):
+    """A batch holding a mesh with holes (winding-number sign, caps built on the device before the
+    launch sequence) is captured once and replayed, with the same grids."""
+    import sdfb
+    from sdfb import meshgen as mg
+    v1, f1 = mg.displaced_icosphere(3, 0.3, 13)
+    v2, f2 = mg.delete_faces(*mg.displaced_torus(30, 10, 0.25, 0.09, 14), 0.06, 15)
+    g = sdfb.make_grid((-0.5,) * 3, 1.0 / 28, (28, 28, 28))
+    opts = sdfb.make_opts(sign_mode=sdfb.SIGN_AUTO)
+    runs = []
+    for _ in range(2):
+        st = sdfb.Stats()
+        st.struct_size = sdfb.C.sizeof(sdfb.Stats)
+        runs.append((ctx.bake_batch([(v1, f1), (v2, f2)], [g, g], opts, stats=st), st.graph_replayed))
+    (d0, o0), _ = runs[0]
+    (d1, o1), replayed = runs[1]
+    assert replayed == 1
+    for a, b in zip(d0 + o0, d1 + o1):
+        assert np.array_equal(a, b)
+    assert (d1[1] < 0).any()  # the holey torus has inside cells (winding-number sign)
