@@ -377,7 +377,7 @@ __global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a, const uint64_t *_
     const MeshRec &M = B.recs[mesh];
     const GridDev g = M.g;
     const float fz = cell_center(g.oz, vz, g.voxel);
-    const double qx = cell_center(g.ox, vx, g.voxel), qy = cell_center(g.oy, vy, g.voxel), qz = fz;
+    const float qx = cell_center(g.ox, vx, g.voxel), qy = cell_center(g.oy, vy, g.voxel);
     double wex[1] = {0.0}, eps[1] = {0.0};
     const float qzs[1] = {fz};
     // lanes of one warp may belong to different meshes: walk each distinct mesh in turn
@@ -385,7 +385,7 @@ __global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a, const uint64_t *_
     const bool uniform = __all_sync(kFull, mesh == first_mesh);
     if (uniform) {
       const bool act[1] = {active};
-      if (M.cap_root >= 0) caps_walk<double, true, 1>(a, M, act, float(qx), float(qy), qzs, tau, wex, eps, corrupt);
+      if (M.cap_root >= 0) caps_walk<double, true, 1>(a, M, act, qx, qy, qzs, tau, wex, eps, corrupt);
     } else {
       unsigned pending = __ballot_sync(kFull, true);
       while (pending) {
@@ -395,7 +395,7 @@ __global__ __launch_bounds__(kThreads) void k_gwn64(GwnArgs a, const uint64_t *_
         const MeshRec &MM = B.recs[mm];
         const bool act[1] = {active && mine};
         if (MM.cap_root >= 0)
-            caps_walk<double, true, 1>(a, MM, act, float(qx), float(qy), qzs, tau, wex, eps, corrupt);
+            caps_walk<double, true, 1>(a, MM, act, qx, qy, qzs, tau, wex, eps, corrupt);
         pending &= ~__ballot_sync(kFull, mine);
       }
     }
